@@ -1,0 +1,460 @@
+#!/usr/bin/env python
+"""SVGF denoiser benchmark: 4K frames/s, HBM roofline fraction, end-to-end rate.
+
+Workload (one "step" = one frame of the chain): the FULL SVGF (5 a-trous
+levels, sigma_l 4 / sigma_n 128 / sigma_z 1, alpha 0.2) at 3840x2160 with
+FP32 storage on a seeded synthetic 60-frame sequence (camera yaw 0.5 deg/frame
++ 0.05 m/frame, a plane appearing at frame 30), inputs RGBA32F radiance, R32F
+depth, RGB32F normals, RG32F motion.  Steps cycle through the sequence; the
+wrap from the last frame to the first is a camera cut (a full disocclusion).
+Every frame's inputs (332 MB) and the state (664 MB) exceed the 126 MB L2, so
+no explicit L2 flush is needed between steps.
+
+  value : frames/s with inputs resident in HBM, device-timed with CUDA events
+  e2e   : frames/s through the host-memory C-ABI call (tg_svgf_denoise_host):
+          pinned host inputs copied in and the result copied out every step
+  roofline : the dominant kernel family's compulsory bytes / its CUDA-event time
+  cpu_baseline : the CPU oracle (float32 FULL port, OpenMP over rows) on the
+          same frames, bounded to ~15 s
+
+Multi-GPU: replicas only (every rank denoises its own stream; no collective on
+the data path); value = frames of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "4K SVGF frames/s + % HBM roofline; batched p50/p99 ms vs plain at ≤1e-3 rel err"
+KEYS = ("radiance", "depth", "normal", "motion")
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=("tg", "reference"), default="tg")
+    ap.add_argument("--width", type=int, default=3840)
+    ap.add_argument("--height", type=int, default=2160)
+    ap.add_argument("--mode", choices=("full", "ref"), default="full")
+    ap.add_argument("--storage", choices=("fp32", "fp16"), default="fp32")
+    ap.add_argument("--pool", type=int, default=60, help="distinct frames generated (the sequence length)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-profile", action="store_true", help="no per-kernel events in the timed region")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args(argv)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        idx = {r[0] for r in rows}
+        want = str(self.gpu_index) if str(self.gpu_index) in idx else rows[0][0]
+        rows = [r for r in rows if r[0] == want]
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world, device):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(v, world, device):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def workload(args):
+    from tron_grid_gb300 import scene
+
+    spec = scene.config1(args.width, args.height, seed=0)
+    name = (f"{'FULL' if args.mode == 'full' else 'REF_EXACT'} SVGF {args.width}x{args.height}, "
+            f"{args.storage.upper()} storage, {5 if args.mode == 'full' else 3} a-trous levels, "
+            f"{args.pool}-frame synthetic sequence (yaw 0.5 deg + 0.05 m per frame, plane appears at frame 30)")
+    return spec, name
+
+
+def gen_frames(spec, n, dev, storage, mode):
+    import torch
+
+    from tron_grid_gb300 import scene
+
+    sc = scene.PlaneScene(spec, device=dev)
+    frames = []
+    for t in range(n):
+        fr = sc.frame(t)
+        d = {k: fr[k] for k in KEYS}
+        if storage == "fp16":
+            d["radiance"] = d["radiance"].to(torch.float16)
+            d["normal"] = scene.oct16_encode(d["normal"])
+        if mode == "ref":
+            d = {"radiance": d["radiance"]}
+        frames.append(d)
+    torch.cuda.synchronize()
+    return frames
+
+
+def algo_bytes_per_px(mode, storage):
+    """Compulsory bytes per pixel of the whole chain: inputs once, state read + written once, output once."""
+    if mode == "full":
+        if storage == "fp32":
+            inputs, state, out = 16 + 4 + 12 + 8, 16 + 16 + 8, 16
+        else:
+            inputs, state, out = 8 + 4 + 4 + 8, 8 + 8 + 4, 8
+        return inputs + 2 * state + out
+    if storage == "fp32":
+        return 16 + 2 * 8 + 16
+    return 8 + 2 * 4 + 8
+
+
+def run_tg(args, rank, world, local):
+    import torch
+
+    import tron_grid_gb300 as tg
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    spec, name = workload(args)
+    W, H = spec.width, spec.height
+    mode = tg.MODE_FULL if args.mode == "full" else tg.MODE_REF_EXACT
+    storage = tg.STORAGE_FP32 if args.storage == "fp32" else tg.STORAGE_FP16
+    frames = gen_frames(spec, args.pool, dev, args.storage, args.mode)
+    out_dt = torch.float32 if args.storage == "fp32" else torch.float16
+    outs = [torch.empty((H, W, 4), dtype=out_dt, device=dev) for _ in range(2)]
+    den = tg.Denoiser(W, H, mode=mode, storage=storage, device=local)
+    kpf = den.info()["kernels_per_frame"]
+    stream = torch.cuda.current_stream()
+
+    def step(i):
+        fr = frames[i % len(frames)]
+        den.denoise(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=outs[i & 1])
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = Clocks(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] if world == 1 else local)
+    clocks.start()
+    if not args.no_profile:
+        den.profile(True)
+        den.profile_read(reset=True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
+        step(args.warmup + i)
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = evs[0].elapsed_time(evs[-1])
+    per = sorted(evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps))
+    prof = den.profile_read(reset=True) if not args.no_profile else {}
+    den.profile(False)
+    t_max = max_over_ranks(total_ms, world, dev)
+    frames_all = sum_over_ranks(float(args.steps), world, dev)
+    value = frames_all / (t_max / 1000.0)
+    px = W * H
+
+    res = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": name, "width": W, "height": H, "mode": args.mode, "storage": args.storage,
+                      "parallelism": f"replicas{world}" if world > 1 else "single",
+                      "l2": "no flush: every frame's inputs (332 MB FP32) and state exceed the 126 MB L2",
+                      "frames_in_pool": args.pool},
+           "mpx_per_s": value * px / 1e6,
+           "p50_ms": per[len(per) // 2], "p99_ms": per[min(len(per) - 1, int(0.99 * len(per)))],
+           "gpu_launches": kpf * args.steps}
+    peak, peak_src = load_peaks()
+    chain_bytes = algo_bytes_per_px(args.mode, args.storage) * px
+    res["chain_roofline"] = {"algo_bytes_per_px": algo_bytes_per_px(args.mode, args.storage),
+                             "achieved": chain_bytes / (res["ms_per_step"] / 1e3) / 1e9, "peak": peak,
+                             "unit": "GB/s", "peak_source": peak_src}
+    res["chain_roofline"]["frac"] = res["chain_roofline"]["achieved"] / peak
+    if prof:
+        kern = {}
+        for k, v in prof.items():
+            ms = v["total_ms"] / max(v["launches"], 1)
+            kern[k] = {"launches": v["launches"], "avg_ms": ms, "share": v["total_ms"] / max(total_ms, 1e-9),
+                       "gbs": v["algo_bytes"] / max(v["total_ms"], 1e-12) / 1e6}
+        dom = max(prof, key=lambda k: prof[k]["total_ms"])
+        d = prof[dom]
+        achieved = d["algo_bytes"] / (d["total_ms"] / 1e3) / 1e9
+        traffic = load_traffic().get(f"{dom}:{args.mode}:{args.storage}")
+        tr = None
+        if traffic:
+            tr = traffic["dram_bytes_per_px"] * px
+        res["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                           "frac": achieved / peak, "traffic": tr,
+                           "algo_bytes_per_launch": d["algo_bytes"] / d["launches"], "peak_source": peak_src}
+        res["kernels"] = kern
+    res["clocks"] = clk
+    den.close()
+    del outs
+    torch.cuda.synchronize()
+
+    if not args.no_e2e:
+        res["e2e"] = run_e2e(args, frames, dev, mode, storage, world)
+    else:
+        res["e2e"] = None
+    del frames
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_cpu:
+        res["cpu_baseline"] = run_cpu_baseline(args, spec, seconds=args.cpu_seconds)
+    return res
+
+
+def run_e2e(args, frames, dev, mode, storage, world):
+    """Frames/s through tg_svgf_denoise_host with pinned host buffers (copies in the timed region)."""
+    import torch
+
+    import tron_grid_gb300 as tg
+
+    n_host = min(8, len(frames))
+    host = [{k: v.cpu().pin_memory() for k, v in frames[i].items()} for i in range(n_host)]
+    W, H = args.width, args.height
+    out_dt = torch.float32 if args.storage == "fp32" else torch.float16
+    houts = [torch.empty((H, W, 4), dtype=out_dt, pin_memory=True) for _ in range(2)]
+    den = tg.Denoiser(W, H, mode=mode, storage=storage, device=dev.index)
+    h2d = sum(v.numel() * v.element_size() for v in host[0].values())
+    d2h = houts[0].numel() * houts[0].element_size()
+
+    def step(i):
+        fr = host[i % n_host]
+        den.denoise_host(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=houts[i & 1])
+
+    for i in range(max(3, min(args.warmup, 8))):
+        step(i)
+    den.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    steps = args.steps
+    t0 = time.perf_counter()
+    for i in range(steps):
+        step(i)
+    den.synchronize()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    barrier(world)
+    el = max_over_ranks(t1 - t0, world, dev)
+    total = sum_over_ranks(float(steps), world, dev)
+    den.close()
+    return {"value": total / el, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": el / steps * 1e3, "host_frames_cycled": n_host,
+            "api": "tg_svgf_denoise_host (pinned host buffers, double-buffered staging)"}
+
+
+def run_cpu_baseline(args, spec, seconds=15.0, frames=None):
+    """The float32 FULL oracle (a port of the path, OpenMP over rows) on the workload's own frames."""
+    import numpy as np
+
+    import oracle
+    from tron_grid_gb300 import scene
+
+    sc = scene.PlaneScene(spec, device="cpu")
+    W, H = spec.width, spec.height
+    if args.mode == "full":
+        P = oracle.full_params()
+        st = oracle.FullState(H, W, np.float32)
+    else:
+        mom = np.zeros((H, W, 2), np.float32)
+    done, el, t = 0, 0.0, 0
+    while True:
+        fr = sc.frame(t)
+        arrs = [fr[k].numpy() for k in KEYS]
+        if args.storage == "fp16":
+            arrs[0] = arrs[0].astype(np.float16).astype(np.float32)
+        t0 = time.perf_counter()
+        if args.mode == "full":
+            oracle.full_frame(P, st, *arrs, fp16_store=args.storage == "fp16")
+        else:
+            _, mom = oracle.ref_frame(arrs[0], mom, fp16_store=args.storage == "fp16")
+        el += time.perf_counter() - t0
+        done += 1
+        t += 1
+        if (frames is not None and done >= frames) or (frames is None and el >= seconds):
+            break
+    return {"value": done / el, "unit": "frames/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"frames 0..{done - 1} of the same {W}x{H} sequence ({el:.1f} s of CPU time, input "
+                      f"generation excluded)"}
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the oracle port of the path on the host cores (the reference's shader cannot run here)."""
+    if rank != 0:
+        return None
+    spec, name = workload(args)
+    import oracle
+
+    # Each step is one frame of the same sequence on all host threads; the step
+    # count is bounded so that the run ends within a few minutes.
+    steps = max(1, min(args.steps, 10))
+    warm = max(0, min(args.warmup, 1))
+    if warm:
+        run_cpu_baseline(args, spec, seconds=0.0, frames=warm)
+    base = run_cpu_baseline(args, spec, seconds=0.0, frames=steps)
+    v = base["value"]
+    res = {"metric": METRIC, "impl": "reference", "value": v, "unit": "frames/s", "n_gpus": world, "steps": steps,
+           "warmup": warm, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": name, "width": spec.width, "height": spec.height, "mode": args.mode,
+                      "storage": args.storage},
+           "cpu_baseline": base, "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    if args.mode == "full":
+        res["note"] = ("the reference has no code for the FULL path (its shader stops before reprojection); the "
+                       "timed CPU implementation is the oracle port of the FULL algorithm")
+    if oracle.reference_available():
+        import numpy as np
+
+        from tron_grid_gb300 import scene
+
+        sc = scene.PlaneScene(spec)
+        raw = sc.frame(0)["radiance"].numpy().astype(np.float16).astype(np.float32)
+        mom = np.zeros((spec.height, spec.width, 2), np.float32)
+        t0 = time.perf_counter()
+        n = 0
+        while n < 2:
+            _, mom = oracle.ref_frame_reference(raw, mom)
+            n += 1
+        dt = time.perf_counter() - t0
+        res["reference_shader_exact"] = {"value": n / dt, "unit": "frames/s",
+                                         "what": "src/svgf_denoise.slang compiled as C++ (reference constants, "
+                                                 "fp16 images), same resolution"}
+    return res
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_tg(args, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

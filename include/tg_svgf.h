@@ -1,0 +1,218 @@
+/*
+ * tg_svgf.h - C ABI of the GB300-native SVGF denoiser.
+ *
+ * This is the drop-in boundary for TronGrid's SVGF combined-lighting pass.  In
+ * the reference the pass is a Vulkan compute pipeline: one shader entry point
+ * `svgfMain` (src/svgf_denoise.slang:152-275) dispatched four times per frame
+ * with a 16-byte push block {width, height, pass_id, stride}
+ * (src/main.cpp:262-269, :906-947) over seven engine-owned images
+ * (src/main.cpp:1326-1397) that are zeroed at start-up and on resize
+ * (src/main.cpp:1399-1496, :1547-1603) and bound in frame-parity descriptor
+ * sets (src/main.cpp:2401-2446).  Here the same pass is one call per frame on
+ * a CUDA stream; the handle owns the history / moments / scratch images and
+ * the caller owns the per-frame inputs and outputs.
+ *
+ * Conventions
+ *  - Every call returns a tg_status; no call throws across the ABI.  After a
+ *    failure tg_last_error() returns a message for the calling thread.
+ *  - A handle is not thread-safe: calls on one handle must be serialised by the
+ *    caller.  Distinct handles may be used concurrently.  Work is ordered on
+ *    the stream passed in (NULL = the CUDA legacy default stream).
+ *  - Images are linear, row-major, pitched device buffers (tg_image).
+ *    pitch_bytes == 0 means tightly packed.  The base address and pitch of a
+ *    4 x float32 image must be multiples of 16 bytes, of a 4 x binary16 image
+ *    multiples of 8, of every other format multiples of 4.
+ */
+#ifndef TG_SVGF_H
+#define TG_SVGF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TG_SVGF_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define TG_API __attribute__((visibility("default")))
+#else
+#define TG_API
+#endif
+
+typedef enum tg_status {
+    TG_OK = 0,
+    TG_ERR_INVALID = 1,     /* bad argument, descriptor, format, pitch or alignment */
+    TG_ERR_OOM = 2,         /* a device or host allocation failed */
+    TG_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    TG_ERR_TIMEOUT = 4,     /* a bounded wait (device or host side) gave up */
+    TG_ERR_BUDGET = 5,      /* serving: the request does not fit the HBM budget */
+    TG_ERR_UNSUPPORTED = 6, /* valid but unimplemented combination */
+    TG_ERR_STATE = 7        /* the object is not in a state that allows the call */
+} tg_status;
+
+typedef enum tg_format {
+    TG_FMT_NONE = 0,
+    TG_FMT_RGBA32F = 1, /* 4 x float32 (16 B/px) */
+    TG_FMT_RGBA16F = 2, /* 4 x binary16 (8 B/px): the reference's rgba16f */
+    TG_FMT_R32F = 3,    /* 1 x float32: linear view-space depth */
+    TG_FMT_RGB32F = 4,  /* 3 x float32 (12 B/px): unit normal */
+    TG_FMT_OCT16 = 5,   /* 2 x snorm16 octahedral unit normal (4 B/px) */
+    TG_FMT_RG32F = 6,   /* 2 x float32: motion vector */
+    TG_FMT_RG16F = 7    /* 2 x binary16: motion vector */
+} tg_format;
+
+typedef struct tg_image {
+    void* ptr;           /* address of row 0, pixel 0 */
+    int64_t pitch_bytes; /* bytes between rows; 0 = width * pixel size */
+    int32_t format;      /* tg_format */
+    int32_t reserved;
+} tg_image;
+
+typedef enum tg_svgf_mode {
+    /* The reference shader exactly: moments EMA + sqrt-variance init pass, then
+     * `levels` (3) a-trous passes at strides 1, 2, 4 with the luminance-only
+     * edge stop, clamp-to-edge taps and unchanged variance propagation
+     * (src/svgf_denoise.slang:176-274).  Uses only inputs.radiance. */
+    TG_SVGF_MODE_REF_EXACT = 0,
+    /* Schied et al. 2017 SVGF: motion-vector reprojection with a bilinear 2x2
+     * history fetch and depth/normal consistency test, history length, colour
+     * and moment EMA, 7x7 spatial variance for short histories, `levels` (5)
+     * a-trous levels with luminance/normal/depth edge stops and squared-weight
+     * variance propagation; level 0 writes the colour history. */
+    TG_SVGF_MODE_FULL = 1
+} tg_svgf_mode;
+
+typedef enum tg_svgf_storage {
+    TG_SVGF_STORAGE_FP32 = 0, /* history, moments and scratch in float32 */
+    TG_SVGF_STORAGE_FP16 = 1  /* binary16 colour/moments, octahedral 2x16-bit normals;
+                                 REF_EXACT: the reference's rgba16f/rg16f images */
+} tg_svgf_storage;
+
+/* The reference's compile-time constants (src/svgf_denoise.slang:118, :137,
+ * :144, :150 and the pass count of src/main.cpp:929) as a runtime block. */
+typedef struct tg_svgf_params {
+    int32_t mode;             /* tg_svgf_mode */
+    int32_t storage;          /* tg_svgf_storage */
+    int32_t levels;           /* a-trous levels, 1..10; reference: 3 */
+    int32_t max_history;      /* FULL: history length cap (>= 1) */
+    int32_t fallback_frames;  /* FULL: 7x7 spatial variance while history < this */
+    int32_t reserved0;
+    float alpha;              /* FULL: colour EMA weight */
+    float moments_alpha;      /* moment EMA weight; reference ALPHA_MOMENTS = 0.2 */
+    float sigma_l;            /* FULL: luminance edge stop; REF_EXACT: SIGMA_COLOR_BASE = 2 */
+    float sigma_n;            /* FULL: normal edge-stop exponent */
+    float sigma_z;            /* FULL: depth edge-stop scale */
+    float variance_epsilon;   /* REF_EXACT: VARIANCE_EPSILON = 1e-4 */
+    float reserved[4];
+} tg_svgf_params;
+
+typedef struct tg_svgf_desc {
+    uint32_t width;
+    uint32_t height;
+    tg_svgf_params params;
+    int32_t device; /* CUDA device ordinal; -1 = the calling thread's current device */
+    int32_t flags;  /* 0 */
+} tg_svgf_desc;
+
+/* Per-frame inputs.  REF_EXACT reads only `radiance` (the reference's
+ * lighting_raw, src/svgf_denoise.slang:61-63).  FULL also reads depth (R32F),
+ * normal (RGB32F / RGBA32F / OCT16, world space, unit length) and motion
+ * (RG32F / RG16F: the offset in pixels from this pixel's centre to the same
+ * surface point's position in the previous frame). */
+typedef struct tg_svgf_inputs {
+    tg_image radiance; /* RGBA32F or RGBA16F; alpha ignored */
+    tg_image depth;
+    tg_image normal;
+    tg_image motion;
+} tg_svgf_inputs;
+
+/* Per-frame output: the reference's denoised_indirect image
+ * (src/svgf_denoise.slang:92-94, written with alpha = 1 at :264-267). */
+typedef struct tg_svgf_outputs {
+    tg_image denoised; /* RGBA32F or RGBA16F */
+} tg_svgf_outputs;
+
+typedef struct tg_svgf_info {
+    uint32_t width;
+    uint32_t height;
+    uint64_t frame_index;       /* frames denoised since create / reset / resize */
+    uint64_t state_bytes;       /* device bytes of persistent state (history, moments, guide) */
+    uint64_t scratch_bytes;     /* device bytes of per-frame scratch */
+    uint64_t staging_bytes;     /* device bytes of host-call staging (0 until first host call) */
+    uint32_t kernels_per_frame; /* kernel launches per tg_svgf_denoise */
+    uint32_t reserved;
+} tg_svgf_info;
+
+typedef struct tg_svgf tg_svgf;
+
+/* Fills `out` with the defaults of a mode: REF_EXACT reproduces the reference
+ * constants; FULL uses sigma_l 4, sigma_n 128, sigma_z 1, alpha 0.2,
+ * moments_alpha 0.2, 5 levels, history cap 32, fallback below 4 frames. */
+TG_API int tg_svgf_params_default(int32_t mode, int32_t storage, tg_svgf_params* out);
+
+/* Allocates and zeroes the handle's state (replaces image creation,
+ * src/main.cpp:1326-1397, the zero clear, :1399-1496, and pipeline /
+ * descriptor creation, :2288-2446).  Synchronises the device once. */
+TG_API int tg_svgf_create(const tg_svgf_desc* desc, tg_svgf** out);
+
+/* Denoises one frame on `stream` (a cudaStream_t): replaces the SVGF block of
+ * recordFrame, src/main.cpp:906-947.  Reads the previous frame's state, writes
+ * this frame's state, writes outputs->denoised.  Asynchronous. */
+TG_API int tg_svgf_denoise(tg_svgf* h, const tg_svgf_inputs* inputs, const tg_svgf_outputs* outputs, void* stream);
+
+/* As tg_svgf_denoise, with inputs and output in HOST memory.  Copies the inputs
+ * to handle-owned device staging, denoises and copies the result back, all
+ * ordered after prior work on `stream`; returns before the copies finish.
+ * The caller keeps the host buffers alive and unmodified until `stream` is
+ * synchronised.  Host buffers should be page-locked for the copies to overlap
+ * with compute; the staging is double-buffered so consecutive frames overlap. */
+TG_API int tg_svgf_denoise_host(tg_svgf* h, const tg_svgf_inputs* host_inputs, const tg_svgf_outputs* host_outputs,
+                         void* stream);
+
+/* Waits until every host copy issued by tg_svgf_denoise_host on this handle
+ * has landed in host memory (the compute is ordered on the caller's stream). */
+TG_API int tg_svgf_synchronize(tg_svgf* h);
+
+/* Zeroes all history: the next frame is a full disocclusion (replaces the
+ * zero clear of src/main.cpp:1399-1496).  Ordered on `stream`. */
+TG_API int tg_svgf_reset(tg_svgf* h, void* stream);
+
+/* Reallocates the state for a new resolution and zeroes it (replaces
+ * rebuildFrameBuffers, src/main.cpp:1547-1603).  Synchronises the device. */
+TG_API int tg_svgf_resize(tg_svgf* h, uint32_t width, uint32_t height);
+
+TG_API int tg_svgf_get_info(const tg_svgf* h, tg_svgf_info* info);
+
+/* Frees everything the handle owns after waiting for its work.  NULL is a no-op. */
+TG_API void tg_svgf_destroy(tg_svgf* h);
+
+TG_API const char* tg_status_string(int status);
+TG_API const char* tg_last_error(void);
+
+/* Per-kernel timing.  While enabled, every kernel launch of tg_svgf_denoise /
+ * tg_svgf_denoise_host is bracketed by a CUDA event pair on the launch stream;
+ * tg_svgf_profile_read waits for those events and returns, per kernel family,
+ * the launch count, the summed event time and the summed compulsory bytes
+ * (each buffer the kernel must read or write, counted once per pixel). */
+typedef struct tg_svgf_kernel_stat {
+    char name[32];     /* "ref_init", "ref_level", "full_temporal", "full_variance", "full_level" */
+    uint32_t launches;
+    uint32_t reserved;
+    double total_ms;
+    double algo_bytes;
+} tg_svgf_kernel_stat;
+
+TG_API int tg_svgf_profile_enable(tg_svgf* h, int enable);
+TG_API int tg_svgf_profile_read(tg_svgf* h, tg_svgf_kernel_stat* stats, int capacity, int* count, int reset);
+
+/* Bytes of device state a FULL or REF_EXACT stream of w x h keeps resident
+ * (history, moments, guide), for admission control. */
+TG_API uint64_t tg_svgf_state_bytes(const tg_svgf_params* params, uint32_t width, uint32_t height);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* TG_SVGF_H */

@@ -1,0 +1,171 @@
+"""ctypes front end of the CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module; the product never imports it.  Arrays are numpy, row-major (h, w, c).
+
+* ``ref_frame``  - restatement of the reference shader chain
+  (`src/svgf_denoise.slang:152-275`, host order `src/main.cpp:929-944`).
+* ``ref_frame_reference`` - the reference shader source itself compiled as C++
+  (oracle/build.py), when the translation could be built.
+* ``full_frame`` - the full Schied-2017 SVGF superset, float32 or float64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_orc = None
+_ref = None
+
+
+class FullParams(C.Structure):
+    _fields_ = [
+        ("alpha", C.c_double),
+        ("moments_alpha", C.c_double),
+        ("sigma_l", C.c_double),
+        ("sigma_n", C.c_double),
+        ("sigma_z", C.c_double),
+        ("levels", C.c_int32),
+        ("max_history", C.c_int32),
+        ("fallback_frames", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+def full_params(alpha=0.2, moments_alpha=0.2, sigma_l=4.0, sigma_n=128.0, sigma_z=1.0, levels=5, max_history=32,
+                fallback_frames=4) -> FullParams:
+    return FullParams(alpha, moments_alpha, sigma_l, sigma_n, sigma_z, levels, max_history, fallback_frames, 0)
+
+
+def _lib():
+    global _orc
+    if _orc is None:
+        path = _build.ORC_LIB
+        if not os.path.exists(path):
+            path = _build.build_oracle()
+        _orc = C.CDLL(path)
+        P = C.c_void_p
+        _orc.orc_ref_frame_f32.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_float, C.c_float, C.c_float,
+                                           C.c_int, C.c_int]
+        _orc.orc_ref_frame_f64.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_double, C.c_double,
+                                           C.c_double, C.c_int, C.c_int]
+        for nm in ("orc_full_frame_f32", "orc_full_frame_f64"):
+            getattr(_orc, nm).argtypes = [C.POINTER(FullParams), C.c_int, C.c_int] + [P] * 12 + [C.c_int, C.c_int]
+        _orc.orc_oct16_encode.argtypes = [C.c_int, P, P]
+        _orc.orc_oct16_decode.argtypes = [C.c_int, P, P]
+        _orc.orc_num_threads.restype = C.c_int
+    return _orc
+
+
+def reference_available() -> bool:
+    return _reflib() is not None
+
+
+def _reflib():
+    global _ref
+    if _ref is None:
+        path = _build.REF_LIB
+        if not os.path.exists(path):
+            try:
+                path = _build.build_reference()
+            except Exception:
+                path = None
+        if path is None or not os.path.exists(path):
+            return None
+        _ref = C.CDLL(path)
+        P = C.c_void_p
+        _ref.ref_svgf_frame.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_int]
+    return _ref
+
+
+def num_threads() -> int:
+    return int(_lib().orc_num_threads())
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def ref_frame(raw, mom_prev, levels=3, phi=2.0, alpha_m=0.2, var_eps=1e-4, fp16_store=True, dtype=np.float32,
+              threads=0):
+    """One reference frame.  raw (h,w,4), mom_prev (h,w,2) -> (out (h,w,4), mom_curr (h,w,2))."""
+    raw = _c(raw, dtype)
+    mom_prev = _c(mom_prev, dtype)
+    h, w = raw.shape[:2]
+    out = np.zeros((h, w, 4), dtype)
+    mom = np.zeros((h, w, 2), dtype)
+    f = _lib().orc_ref_frame_f32 if dtype == np.float32 else _lib().orc_ref_frame_f64
+    rc = f(w, h, _p(raw), _p(mom_prev), _p(mom), _p(out), levels, phi, alpha_m, var_eps, int(bool(fp16_store)),
+           threads)
+    if rc:
+        raise ValueError("oracle ref_frame rejected its arguments")
+    return out, mom
+
+
+def ref_frame_reference(raw, mom_prev, fp16_store=True, threads=0):
+    """The reference shader itself (compiled as C++): init + 3 levels."""
+    lib = _reflib()
+    if lib is None:
+        raise RuntimeError("reference shader translation not built (oracle/_ref)")
+    raw = _c(raw, np.float32).copy()
+    mom_prev = _c(mom_prev, np.float32).copy()
+    h, w = raw.shape[:2]
+    out = np.zeros((h, w, 4), np.float32)
+    mom = np.zeros((h, w, 2), np.float32)
+    rc = lib.ref_svgf_frame(w, h, _p(raw), _p(mom_prev), _p(mom), _p(out), int(bool(fp16_store)), threads)
+    if rc:
+        raise ValueError("reference frame rejected its arguments")
+    return out, mom
+
+
+class FullState:
+    """Per-stream state of the FULL oracle (zero = no history)."""
+
+    def __init__(self, h, w, dtype=np.float64):
+        self.guide = np.zeros((h, w, 4), dtype)
+        self.hist = np.zeros((h, w, 4), dtype)
+        self.mom = np.zeros((h, w, 2), dtype)
+
+
+def full_frame(params: FullParams, state: FullState, radiance, depth, normal, motion, fp16_store=False, threads=0):
+    """One FULL frame; updates ``state`` in place and returns (out (h,w,4), var (h,w))."""
+    dt = state.guide.dtype
+    radiance = _c(radiance, dt)
+    depth = _c(depth, dt)
+    normal = _c(normal, dt)
+    motion = _c(motion, dt)
+    h, w = depth.shape[:2]
+    g = np.zeros_like(state.guide)
+    hs = np.zeros_like(state.hist)
+    m = np.zeros_like(state.mom)
+    out = np.zeros((h, w, 4), dt)
+    var = np.zeros((h, w), dt)
+    f = _lib().orc_full_frame_f32 if dt == np.float32 else _lib().orc_full_frame_f64
+    rc = f(C.byref(params), w, h, _p(radiance), _p(depth), _p(normal), _p(motion), _p(state.guide), _p(state.hist),
+           _p(state.mom), _p(g), _p(hs), _p(m), _p(out), _p(var), int(bool(fp16_store)), threads)
+    if rc:
+        raise ValueError("oracle full_frame rejected its arguments")
+    state.guide, state.hist, state.mom = g, hs, m
+    return out, var
+
+
+def oct16_encode(normals):
+    n = _c(normals, np.float32).reshape(-1, 3)
+    out = np.zeros((n.shape[0], 2), np.int16)
+    _lib().orc_oct16_encode(n.shape[0], _p(n), _p(out))
+    return out.reshape(tuple(np.shape(normals)[:-1]) + (2,))
+
+
+def oct16_decode(enc):
+    e = _c(enc, np.int16).reshape(-1, 2)
+    out = np.zeros((e.shape[0], 3), np.float32)
+    _lib().orc_oct16_decode(e.shape[0], _p(e), _p(out))
+    return out.reshape(tuple(np.shape(enc)[:-1]) + (3,))

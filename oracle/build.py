@@ -1,0 +1,109 @@
+"""Build recipe for the CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+Produces
+  oracle/_build/liborc.so   - the C++ restatement (oracle/svgf_oracle.cpp);
+  oracle/_ref/libsvgf_ref.so - the reference shader `src/svgf_denoise.slang`
+                               compiled as C++ (when its translation exists).
+
+The translation of the shader is made here from the reference checkout, with
+exactly three textual edits that remove Slang-only syntax:
+  * the `[shader("compute")]` attribute line,
+  * the `[numthreads(8, 8, 1)]` attribute line,
+  * the `: SV_DispatchThreadID` parameter semantic.
+Everything else in the shader compiles unchanged against oracle/slang_prelude.hpp.
+The translation is written to oracle/_ref/ (git-ignored, never committed) so
+that a machine without the reference checkout can still compile it.
+
+Usage: python oracle/build.py [--reference-root DIR]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+ORC_LIB = os.path.join(BUILD_DIR, "liborc.so")
+REF_LIB = os.path.join(REF_DIR, "libsvgf_ref.so")
+REF_GEN = os.path.join(REF_DIR, "svgf_denoise_gen.cpp")
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"]
+
+
+def _newer(target: str, *sources: str) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources if os.path.exists(s))
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "svgf_oracle.cpp")
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not _newer(ORC_LIB, src):
+        tmp = ORC_LIB + ".tmp"
+        subprocess.check_call(["g++", *CXXFLAGS, src, "-o", tmp])
+        os.replace(tmp, ORC_LIB)
+    return ORC_LIB
+
+
+def translate_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+    """Write oracle/_ref/svgf_denoise_gen.cpp from the reference shader, if present."""
+    shader = os.path.join(reference_root, "src", "svgf_denoise.slang")
+    if not os.path.isfile(shader):
+        return None
+    with open(shader, encoding="utf-8") as f:
+        text = f.read()
+    out_lines = []
+    removed = 0
+    for line in text.splitlines():
+        s = line.strip()
+        if s == '[shader("compute")]' or re.fullmatch(r"\[numthreads\(\s*8\s*,\s*8\s*,\s*1\s*\)\]", s):
+            removed += 1
+            continue
+        out_lines.append(line)
+    body = "\n".join(out_lines) + "\n"
+    body, nsem = re.subn(r"\s*:\s*SV_DispatchThreadID", "", body)
+    if removed != 2 or nsem != 1:
+        raise RuntimeError(f"unexpected shader layout (attributes removed={removed}, semantics={nsem})")
+    os.makedirs(REF_DIR, exist_ok=True)
+    header = f"// Generated by oracle/build.py from {shader}; not committed.\n"
+    new = header + body
+    if not os.path.exists(REF_GEN) or open(REF_GEN, encoding="utf-8").read() != new:
+        with open(REF_GEN, "w", encoding="utf-8") as f:
+            f.write(new)
+    return REF_GEN
+
+
+def build_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+    """Compile the translated reference shader; None when no translation exists."""
+    translate_reference(reference_root)
+    if not os.path.isfile(REF_GEN):
+        return None
+    drv = os.path.join(HERE, "ref_driver.cpp")
+    pre = os.path.join(HERE, "slang_prelude.hpp")
+    if force or not _newer(REF_LIB, REF_GEN, drv, pre):
+        tmp = REF_LIB + ".tmp"
+        subprocess.check_call(["g++", *CXXFLAGS, "-std=c++20", "-Wno-attributes", "-I", HERE, "-I", REF_DIR, drv, "-o", tmp])
+        os.replace(tmp, REF_LIB)
+    return REF_LIB
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference-root", default=DEFAULT_REFERENCE_ROOT)
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args(argv)
+    print(build_oracle(a.force))
+    r = build_reference(a.force, a.reference_root)
+    print(r if r else "reference shader translation absent: oracle/_ref not built")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,85 @@
+"""The C-ABI library: it loads, exports every symbol include/*.h declares, and
+behaves on host-only paths (no kernel is launched here)."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+import tron_grid_gb300 as tg
+from tron_grid_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        with open(h) as f:
+            txt = f.read()
+        names |= set(re.findall(r"^TG_API\s+[\w\s\*]+?\b(tg_\w+)\s*\(", txt, flags=re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = L.load()
+    declared = _declared()
+    assert len(declared) >= 14
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+    assert declared <= set(L.SIGNATURES), f"ctypes signatures missing: {declared - set(L.SIGNATURES)}"
+
+
+def test_params_defaults_reproduce_reference_constants():
+    p = L.default_params(L.MODE_REF_EXACT, L.STORAGE_FP16)
+    # src/svgf_denoise.slang:137, :144, :150 and src/main.cpp:929
+    assert (p.levels, p.sigma_l, round(p.moments_alpha, 6), round(p.variance_epsilon, 8)) == (3, 2.0, 0.2, 1e-4)
+    f = L.default_params(L.MODE_FULL, L.STORAGE_FP32)
+    assert (f.levels, f.sigma_l, f.sigma_n, f.sigma_z) == (5, 4.0, 128.0, 1.0)
+    assert round(f.alpha, 6) == 0.2 and f.max_history == 32 and f.fallback_frames == 4
+
+
+def test_params_default_rejects_bad_mode():
+    p = L.Params()
+    assert L.load().tg_svgf_params_default(7, 0, C.byref(p)) == L.ERR_INVALID
+    assert b"mode" in L.load().tg_last_error()
+
+
+def test_state_bytes():
+    # FULL FP32: 2 x (guide 16 + history 16 + moments 8) B/px; FP16: 2 x (8 + 8 + 4)
+    assert tg.state_bytes(3840, 2160) == 2 * 40 * 3840 * 2160
+    assert tg.state_bytes(3840, 2160, storage=L.STORAGE_FP16) == 2 * 20 * 3840 * 2160
+    assert tg.state_bytes(1280, 720, mode=L.MODE_REF_EXACT, storage=L.STORAGE_FP16) == 2 * 4 * 1280 * 720
+
+
+def test_create_rejects_bad_descriptors_before_touching_a_device():
+    lib = L.load()
+    h = C.c_void_p()
+    d = L.Desc(0, 10, L.default_params(), 0, 0)
+    assert lib.tg_svgf_create(C.byref(d), C.byref(h)) == L.ERR_INVALID
+    d = L.Desc(16, 16, L.default_params(levels=0), 0, 0)
+    assert lib.tg_svgf_create(C.byref(d), C.byref(h)) == L.ERR_INVALID
+    d = L.Desc(16, 16, L.default_params(alpha=0.0), 0, 0)
+    assert lib.tg_svgf_create(C.byref(d), C.byref(h)) == L.ERR_INVALID
+    assert lib.tg_svgf_create(None, C.byref(h)) == L.ERR_INVALID
+    assert not h.value
+
+
+def test_null_handle_calls_fail_cleanly():
+    lib = L.load()
+    assert lib.tg_svgf_denoise(None, None, None, None) == L.ERR_INVALID
+    assert lib.tg_svgf_reset(None, None) == L.ERR_INVALID
+    assert lib.tg_svgf_synchronize(None) == L.ERR_INVALID
+    lib.tg_svgf_destroy(None)
+    assert lib.tg_status_string(L.ERR_BUDGET) == b"over HBM budget"
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(ImportError):
+        L._lib_backup = L._lib
+        L._lib = None
+        try:
+            L.load(str(tmp_path / "nope.so"))
+        finally:
+            L._lib = L._lib_backup

@@ -1,0 +1,207 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Tolerances
+* FP32 storage (both modes): per-pixel relative luminance error <= 1e-4
+  (absolute floor 1e-7) against the oracle evaluated in float32.
+* REF_EXACT with the reference's fp16 images: the GPU rounds to binary16 at
+  every store exactly as the oracle does; a last-bit difference in an
+  exponential can move one stored value by one fp16 step (2^-11 relative), so
+  the bound is 2 fp16 steps per pixel (2^-10) and 99.9% of pixels identical.
+* FULL with FP16 storage: against the float32 oracle with the same fp16 /
+  octahedral storage emulation (per-pixel 2^-8, mean 1e-5), and against the
+  float64 oracle without emulation: relative L2 luminance error <= 1e-3.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import tron_grid_gb300 as tg
+from tron_grid_gb300 import scene
+from tests.helpers import LUM_FLOOR, REL_TOL, rel_err, rel_l2, report
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("radiance", "depth", "normal", "motion")
+
+
+def _frames(spec, n):
+    sc = scene.PlaneScene(spec)
+    return [sc.frame(t) for t in range(n)]
+
+
+def _run_full_pair(dev, spec, n_frames, storage=tg.STORAGE_FP32, fp16_inputs=False, check=None):
+    W, H = spec.width, spec.height
+    den = tg.Denoiser(W, H, mode=tg.MODE_FULL, storage=storage)
+    st32 = oracle.FullState(H, W, np.float32)
+    st64 = oracle.FullState(H, W, np.float64)
+    P = oracle.full_params()
+    f16 = storage == tg.STORAGE_FP16
+    out_dt = torch.float16 if f16 else torch.float32
+    results = []
+    sc = scene.PlaneScene(spec)
+    for t in range(n_frames):
+        fr = sc.frame(t)
+        rad, dep, nrm, mot = (fr[k] for k in KEYS)
+        nrm_np = nrm.numpy()
+        if fp16_inputs:
+            rad_d = rad.to(torch.float16).to(dev)
+            enc = oracle.oct16_encode(nrm_np)
+            nrm_d = torch.from_numpy(enc).to(dev)
+            rad_np = rad.to(torch.float16).float().numpy()
+            nrm_np = oracle.oct16_decode(enc)
+        else:
+            rad_d, nrm_d = rad.to(dev), nrm.to(dev)
+            rad_np = rad.numpy()
+        out = torch.empty((H, W, 4), dtype=out_dt, device=dev)
+        den.denoise(rad_d, dep.to(dev), nrm_d, mot.to(dev), out=out)
+        g = out.float().cpu().numpy()
+        r32, _ = oracle.full_frame(P, st32, rad_np, dep.numpy(), nrm_np, mot.numpy(), fp16_store=f16)
+        r64, _ = oracle.full_frame(P, st64, rad.numpy(), dep.numpy(), nrm.numpy(), mot.numpy(), fp16_store=False)
+        results.append((g, r32, r64, fr))
+        if check:
+            check(t, g, r32, r64)
+    den.close()
+    return results
+
+
+def _check_fp32(t, g, r32, r64):
+    e = rel_err(g, r32)
+    assert np.all(np.isfinite(g))
+    assert e.max() <= REL_TOL, f"frame {t}: max rel err {e.max():.3e} vs float32 oracle ({report(g, r32)})"
+    assert rel_l2(g, r64) <= 1e-4, f"frame {t}: rel L2 vs float64 {rel_l2(g, r64):.3e}"
+
+
+def test_full_fp32_config0(cuda_dev):
+    """640x360, 8 frames, yaw 0.2 deg/frame, 5 levels, sigma 4/128/1."""
+    _run_full_pair(cuda_dev, scene.config0(seed=1), 8, check=_check_fp32)
+
+
+def test_full_fp32_motion_and_disocclusion(cuda_dev):
+    """Yaw 0.5 deg + 0.05 m per frame with a plane appearing at frame 30 (320x180)."""
+    spec = scene.config1(320, 180, seed=2)
+    _run_full_pair(cuda_dev, spec, 33, check=_check_fp32)
+
+
+@pytest.mark.parametrize("wh", [(1, 1), (2, 2), (7, 3), (33, 17), (5, 40)])
+def test_full_fp32_odd_sizes(cuda_dev, wh):
+    spec = scene.config1(wh[0], wh[1], seed=3)
+    _run_full_pair(cuda_dev, spec, 5, check=_check_fp32)
+
+
+def test_full_fp16_storage(cuda_dev):
+    """FP16 colour/moments, octahedral normals; FP16 radiance + OCT16 normal inputs."""
+    stats = []
+
+    def chk(t, g, r32, r64):
+        e = rel_err(g, r32)
+        assert np.all(np.isfinite(g))
+        assert e.max() <= 2.0 ** -8, f"frame {t}: max rel {e.max():.3e} vs emulating oracle"
+        assert e.mean() <= 1e-5, f"frame {t}: mean rel {e.mean():.3e} vs emulating oracle"
+        l2 = rel_l2(g, r64)
+        stats.append(l2)
+        assert l2 <= 1e-3, f"frame {t}: rel L2 vs float64 oracle {l2:.3e}"
+
+    _run_full_pair(cuda_dev, scene.config1(320, 180, seed=4), 33, storage=tg.STORAGE_FP16, fp16_inputs=True,
+                   check=chk)
+
+
+def _ref_pair(dev, spec, n, storage, check):
+    W, H = spec.width, spec.height
+    den = tg.Denoiser(W, H, mode=tg.MODE_REF_EXACT, storage=storage)
+    f16 = storage == tg.STORAGE_FP16
+    mom = np.zeros((H, W, 2), np.float32)
+    sc = scene.PlaneScene(spec)
+    for t in range(n):
+        raw = sc.frame(t)["radiance"]
+        if f16:
+            raw = raw.to(torch.float16)
+        out = torch.empty((H, W, 4), dtype=raw.dtype, device=dev)
+        den.denoise(raw.to(dev), out=out)
+        ref, mom = oracle.ref_frame(raw.float().numpy(), mom, fp16_store=f16)
+        check(t, out.float().cpu().numpy(), ref)
+    den.close()
+
+
+def test_ref_exact_fp32(cuda_dev):
+    def chk(t, g, r):
+        e = rel_err(g, r)
+        assert e.max() <= REL_TOL, f"frame {t}: {report(g, r)}"
+        assert np.all(g[..., 3] == 1.0)
+
+    _ref_pair(cuda_dev, scene.config0(seed=5), 8, tg.STORAGE_FP32, chk)
+
+
+def test_ref_exact_fp16_images(cuda_dev):
+    """The reference's rgba16f / rg16f images (moments overflow to inf/NaN above luminance ~256, as in the reference)."""
+    def chk(t, g, r):
+        d = np.abs(g[..., :3] - r[..., :3]) / np.maximum(np.abs(r[..., :3]), 2.0 ** -14)
+        assert d.max() <= 2.0 ** -10, f"frame {t}: max rel {d.max():.3e}"
+        same = np.mean(g[..., :3] == r[..., :3])
+        assert same >= 0.999, f"frame {t}: only {same:.5f} of values identical"
+
+    _ref_pair(cuda_dev, scene.config0(seed=6), 8, tg.STORAGE_FP16, chk)
+
+
+@pytest.mark.parametrize("wh", [(1, 1), (2, 2), (7, 3), (33, 17)])
+def test_ref_exact_odd_sizes(cuda_dev, wh):
+    def chk(t, g, r):
+        assert rel_err(g, r).max() <= REL_TOL
+
+    _ref_pair(cuda_dev, scene.SceneSpec(wh[0], wh[1], seed=8), 4, tg.STORAGE_FP32, chk)
+
+
+def test_host_api_matches_device_api(cuda_dev):
+    spec = scene.config1(200, 120, seed=9)
+    frames = _frames(spec, 4)
+    a = tg.Denoiser(200, 120)
+    b = tg.Denoiser(200, 120)
+    outs_h = []
+    for fr in frames:
+        ins = [fr[k].pin_memory() for k in KEYS]
+        outs_h.append(b.denoise_host(*ins))
+    b.synchronize()
+    for fr, oh in zip(frames, outs_h):
+        od = a.denoise(*(fr[k].to(cuda_dev) for k in KEYS))
+        assert torch.equal(od.cpu(), oh)
+    a.close()
+    b.close()
+
+
+def test_reset_restarts_history(cuda_dev):
+    spec = scene.config1(64, 48, seed=10)
+    frames = _frames(spec, 3)
+    d = tg.Denoiser(64, 48)
+    first = d.denoise(*(frames[0][k].to(cuda_dev) for k in KEYS)).cpu()
+    d.denoise(*(frames[1][k].to(cuda_dev) for k in KEYS))
+    d.reset()
+    again = d.denoise(*(frames[0][k].to(cuda_dev) for k in KEYS)).cpu()
+    assert torch.equal(first, again)
+    assert d.info()["frame_index"] == 1
+    d.close()
+
+
+def test_input_layouts_agree(cuda_dev):
+    """RGB32F vs RGBA32F vs pitched normals and pitched radiance give identical output."""
+    W, H = 48, 40
+    fr = _frames(scene.config1(W, H, seed=11), 1)[0]
+    rad, dep, nrm, mot = (fr[k].to(cuda_dev) for k in KEYS)
+    base = tg.Denoiser(W, H).denoise(rad, dep, nrm, mot).cpu()
+    nrm4 = torch.cat([nrm, torch.zeros_like(nrm[..., :1])], -1)
+    assert torch.equal(tg.Denoiser(W, H).denoise(rad, dep, nrm4, mot).cpu(), base)
+    wide = torch.zeros((H, W + 7, 4), device=cuda_dev)
+    wide[:, :W] = rad
+    assert torch.equal(tg.Denoiser(W, H).denoise(wide[:, :W], dep, nrm, mot).cpu(), base)
+
+
+def test_invalid_arguments_raise(cuda_dev):
+    d = tg.Denoiser(32, 32)
+    rad = torch.zeros((32, 32, 4), device=cuda_dev)
+    dep = torch.zeros((32, 32), device=cuda_dev)
+    nrm = torch.zeros((32, 32, 3), device=cuda_dev)
+    with pytest.raises(tg.TgError) as e:  # FULL without motion
+        d.denoise(rad, dep, nrm, None)
+    assert e.value.status == tg._lib.ERR_INVALID
+    with pytest.raises(ValueError):
+        d.denoise(rad.double(), dep, nrm, torch.zeros((32, 32, 2), device=cuda_dev))
+    d.close()

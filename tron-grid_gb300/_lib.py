@@ -1,0 +1,119 @@
+"""ctypes declarations of include/tg_svgf.h and the loader of libtg_svgf.so.
+
+The library is the product: if it is missing the import of this package fails
+with an error that says how to build it.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libtg_svgf.so")
+
+# tg_status
+OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_BUDGET, ERR_UNSUPPORTED, ERR_STATE = range(8)
+# tg_format
+FMT_NONE, FMT_RGBA32F, FMT_RGBA16F, FMT_R32F, FMT_RGB32F, FMT_OCT16, FMT_RG32F, FMT_RG16F = range(8)
+FMT_BYTES = {FMT_RGBA32F: 16, FMT_RGBA16F: 8, FMT_R32F: 4, FMT_RGB32F: 12, FMT_OCT16: 4, FMT_RG32F: 8, FMT_RG16F: 4}
+# tg_svgf_mode / tg_svgf_storage
+MODE_REF_EXACT, MODE_FULL = 0, 1
+STORAGE_FP32, STORAGE_FP16 = 0, 1
+
+
+class Image(C.Structure):
+    _fields_ = [("ptr", C.c_void_p), ("pitch_bytes", C.c_int64), ("format", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32), ("storage", C.c_int32), ("levels", C.c_int32), ("max_history", C.c_int32),
+        ("fallback_frames", C.c_int32), ("reserved0", C.c_int32),
+        ("alpha", C.c_float), ("moments_alpha", C.c_float), ("sigma_l", C.c_float), ("sigma_n", C.c_float),
+        ("sigma_z", C.c_float), ("variance_epsilon", C.c_float), ("reserved", C.c_float * 4),
+    ]
+
+
+class Desc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("params", Params), ("device", C.c_int32),
+                ("flags", C.c_int32)]
+
+
+class Inputs(C.Structure):
+    _fields_ = [("radiance", Image), ("depth", Image), ("normal", Image), ("motion", Image)]
+
+
+class Outputs(C.Structure):
+    _fields_ = [("denoised", Image)]
+
+
+class Info(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("frame_index", C.c_uint64),
+                ("state_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64), ("staging_bytes", C.c_uint64),
+                ("kernels_per_frame", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint32), ("reserved", C.c_uint32),
+                ("total_ms", C.c_double), ("algo_bytes", C.c_double)]
+
+
+class TgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+# (name, restype, argtypes) of every entry point declared in include/*.h.
+_P = C.c_void_p
+SIGNATURES = {
+    "tg_svgf_params_default": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(Params)]),
+    "tg_svgf_create": (C.c_int, [C.POINTER(Desc), C.POINTER(_P)]),
+    "tg_svgf_denoise": (C.c_int, [_P, C.POINTER(Inputs), C.POINTER(Outputs), _P]),
+    "tg_svgf_denoise_host": (C.c_int, [_P, C.POINTER(Inputs), C.POINTER(Outputs), _P]),
+    "tg_svgf_synchronize": (C.c_int, [_P]),
+    "tg_svgf_reset": (C.c_int, [_P, _P]),
+    "tg_svgf_resize": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "tg_svgf_get_info": (C.c_int, [_P, C.POINTER(Info)]),
+    "tg_svgf_destroy": (None, [_P]),
+    "tg_status_string": (C.c_char_p, [C.c_int]),
+    "tg_last_error": (C.c_char_p, []),
+    "tg_svgf_state_bytes": (C.c_uint64, [C.POINTER(Params), C.c_uint32, C.c_uint32]),
+    "tg_svgf_profile_enable": (C.c_int, [_P, C.c_int]),
+    "tg_svgf_profile_read": (C.c_int, [_P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int), C.c_int]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads libtg_svgf.so (once) and declares every signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(
+            f"{path} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"` "
+            "(the SVGF denoiser has no CPU fallback)")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int):
+    if status != OK:
+        msg = load().tg_last_error()
+        raise TgError(status, msg.decode() if msg else "tg_svgf error")
+    return status
+
+
+def default_params(mode: int = MODE_FULL, storage: int = STORAGE_FP32, **overrides) -> Params:
+    p = Params()
+    check(load().tg_svgf_params_default(mode, storage, C.byref(p)))
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p

@@ -1,0 +1,746 @@
+// C ABI of the single-stream SVGF denoiser (include/tg_svgf.h).
+//
+// The handle replaces the reference's seven engine-owned images and their
+// frame-parity descriptor sets (src/main.cpp:1326-1397, :2401-2446): it owns
+// the ping-pong state (REF_EXACT: moments; FULL: guide, colour history,
+// moments) and the per-frame scratch, all in one device allocation each, and
+// alternates the ping-pong halves by frame parity exactly as the reference
+// alternates descriptor sets.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "svgf_internal.h"
+#include "svgf_kernels.cuh"
+
+using namespace tg;
+
+namespace tg {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+int fmt_bytes(int fmt)
+{
+    switch (fmt) {
+    case TG_FMT_RGBA32F: return 16;
+    case TG_FMT_RGBA16F: return 8;
+    case TG_FMT_R32F: return 4;
+    case TG_FMT_RGB32F: return 12;
+    case TG_FMT_OCT16: return 4;
+    case TG_FMT_RG32F: return 8;
+    case TG_FMT_RG16F: return 4;
+    default: return 0;
+    }
+}
+
+static int fmt_align(int fmt)
+{
+    switch (fmt) {
+    case TG_FMT_RGBA32F: return 16;
+    case TG_FMT_RGBA16F: return 8;
+    case TG_FMT_RG32F: return 8;
+    default: return 4;
+    }
+}
+
+int check_image(const char* what, const tg_image& im, uint32_t w, uint32_t h, const int* allowed, int n_allowed)
+{
+    bool ok = false;
+    for (int k = 0; k < n_allowed; ++k) ok |= im.format == allowed[k];
+    if (!ok) return fail(TG_ERR_INVALID, "%s: unsupported format %d", what, im.format);
+    if (!im.ptr) return fail(TG_ERR_INVALID, "%s: null pointer", what);
+    const int64_t bpp = fmt_bytes(im.format);
+    const int64_t pitch = im.pitch_bytes ? im.pitch_bytes : bpp * int64_t(w);
+    const int al = fmt_align(im.format);
+    if (pitch < bpp * int64_t(w)) return fail(TG_ERR_INVALID, "%s: pitch %lld below row size", what, (long long)pitch);
+    if ((reinterpret_cast<uintptr_t>(im.ptr) % al) != 0 || (pitch % al) != 0)
+        return fail(TG_ERR_INVALID, "%s: address and pitch must be multiples of %d bytes", what, al);
+    (void)h;
+    return TG_OK;
+}
+
+Img to_img(const tg_image& im, uint32_t w)
+{
+    Img r;
+    r.ptr = static_cast<char*>(im.ptr);
+    r.pitch = im.pitch_bytes ? im.pitch_bytes : int64_t(fmt_bytes(im.format)) * w;
+    r.fmt = im.format;
+    r.pad = 0;
+    return r;
+}
+
+int sigma_n_squarings(float sigma_n)
+{
+    for (int k = 0; k <= 10; ++k)
+        if (sigma_n == float(1 << k)) return k;
+    return -1;
+}
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Bytes per pixel of each handle-owned buffer.
+struct Layout {
+    size_t guide, c4, mom;
+};
+
+static Layout layout_of(const tg_svgf_params& p)
+{
+    const bool f16 = p.storage == TG_SVGF_STORAGE_FP16;
+    Layout l;
+    l.guide = f16 ? 8 : 16;
+    l.c4 = f16 ? 8 : 16;
+    l.mom = f16 ? 4 : 8;
+    return l;
+}
+
+size_t state_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
+{
+    const size_t n = size_t(w) * h;
+    const Layout l = layout_of(p);
+    if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * align_up(n * l.mom, 256);
+    return 2 * (align_up(n * l.guide, 256) + align_up(n * l.c4, 256) + align_up(n * l.mom, 256));
+}
+
+size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
+{
+    const size_t n = size_t(w) * h;
+    const Layout l = layout_of(p);
+    if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * align_up(n * l.c4, 256);
+    return 3 * align_up(n * l.c4, 256);
+}
+
+int validate_params(const tg_svgf_params& p)
+{
+    if (p.mode != TG_SVGF_MODE_REF_EXACT && p.mode != TG_SVGF_MODE_FULL)
+        return fail(TG_ERR_INVALID, "params.mode %d unknown", p.mode);
+    if (p.storage != TG_SVGF_STORAGE_FP32 && p.storage != TG_SVGF_STORAGE_FP16)
+        return fail(TG_ERR_INVALID, "params.storage %d unknown", p.storage);
+    if (p.levels < 1 || p.levels > 10) return fail(TG_ERR_INVALID, "params.levels %d outside 1..10", p.levels);
+    if (p.mode == TG_SVGF_MODE_FULL) {
+        if (p.max_history < 1) return fail(TG_ERR_INVALID, "params.max_history must be >= 1");
+        if (!(p.alpha > 0.0f && p.alpha <= 1.0f)) return fail(TG_ERR_INVALID, "params.alpha outside (0, 1]");
+        if (!(p.moments_alpha > 0.0f && p.moments_alpha <= 1.0f))
+            return fail(TG_ERR_INVALID, "params.moments_alpha outside (0, 1]");
+        if (!(p.sigma_l > 0.0f) || !(p.sigma_n > 0.0f) || !(p.sigma_z > 0.0f))
+            return fail(TG_ERR_INVALID, "params.sigma_* must be positive");
+    } else {
+        if (!(p.moments_alpha >= 0.0f && p.moments_alpha <= 1.0f))
+            return fail(TG_ERR_INVALID, "params.moments_alpha outside [0, 1]");
+        if (!(p.variance_epsilon > 0.0f)) return fail(TG_ERR_INVALID, "params.variance_epsilon must be positive");
+    }
+    return TG_OK;
+}
+
+} // namespace tg
+
+namespace tg {
+enum Family { F_REF_INIT = 0, F_REF_LEVEL, F_FULL_TEMPORAL, F_FULL_VARIANCE, F_FULL_LEVEL, kFamilies };
+static const char* kFamilyName[kFamilies] = {"ref_init", "ref_level", "full_temporal", "full_variance", "full_level"};
+} // namespace tg
+
+struct tg_svgf {
+    int device = 0;
+    uint32_t w = 0, h = 0;
+    tg_svgf_params p{};
+    uint64_t frame = 0;
+    char* state = nullptr;
+    char* scratch = nullptr;
+    size_t state_bytes = 0, scratch_bytes = 0;
+    // carved views
+    void* guide[2] = {nullptr, nullptr};
+    void* hist[2] = {nullptr, nullptr};
+    void* mom[2] = {nullptr, nullptr};
+    void* tc = nullptr;
+    void* colA = nullptr;
+    void* colB = nullptr;
+    // host-call staging (double buffered)
+    struct Staging {
+        char* buf = nullptr;
+        size_t bytes = 0;
+        cudaEvent_t ev_in = nullptr, ev_comp = nullptr, ev_done = nullptr;
+        bool used = false;
+    } stg[2];
+    int stg_next = 0;
+    cudaStream_t copy_stream = nullptr;
+    // per-kernel CUDA-event profiling
+    struct Prof {
+        bool on = false;
+        struct Rec {
+            int fam;
+            double bytes;
+            cudaEvent_t a, b;
+        };
+        std::vector<Rec> pending;
+        std::vector<cudaEvent_t> pool;
+        uint32_t launches[kFamilies] = {};
+        double ms[kFamilies] = {};
+        double bytes[kFamilies] = {};
+    } prof;
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    bool switched = false;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) switched = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard()
+    {
+        if (switched) cudaSetDevice(prev);
+    }
+};
+
+void carve(tg_svgf* s)
+{
+    const size_t n = size_t(s->w) * s->h;
+    const Layout l = layout_of(s->p);
+    char* p = s->state;
+    auto take = [&](size_t bytes) {
+        void* r = p;
+        p += align_up(bytes, 256);
+        return r;
+    };
+    if (s->p.mode == TG_SVGF_MODE_REF_EXACT) {
+        s->mom[0] = take(n * l.mom);
+        s->mom[1] = take(n * l.mom);
+        p = s->scratch;
+        s->colA = take(n * l.c4);
+        s->colB = take(n * l.c4);
+        s->guide[0] = s->guide[1] = s->hist[0] = s->hist[1] = s->tc = nullptr;
+    } else {
+        for (int k = 0; k < 2; ++k) {
+            s->guide[k] = take(n * l.guide);
+            s->hist[k] = take(n * l.c4);
+            s->mom[k] = take(n * l.mom);
+        }
+        p = s->scratch;
+        s->tc = take(n * l.c4);
+        s->colA = take(n * l.c4);
+        s->colB = take(n * l.c4);
+    }
+}
+
+void free_buffers(tg_svgf* s)
+{
+    if (s->state) cudaFree(s->state);
+    if (s->scratch) cudaFree(s->scratch);
+    s->state = s->scratch = nullptr;
+    s->state_bytes = s->scratch_bytes = 0;
+}
+
+void free_staging(tg_svgf* s)
+{
+    for (auto& g : s->stg) {
+        if (g.buf) cudaFree(g.buf);
+        if (g.ev_in) cudaEventDestroy(g.ev_in);
+        if (g.ev_comp) cudaEventDestroy(g.ev_comp);
+        if (g.ev_done) cudaEventDestroy(g.ev_done);
+        g = tg_svgf::Staging{};
+    }
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    s->copy_stream = nullptr;
+}
+
+int alloc_buffers(tg_svgf* s)
+{
+    s->state_bytes = state_bytes_of(s->p, s->w, s->h);
+    s->scratch_bytes = scratch_bytes_of(s->p, s->w, s->h);
+    if (cudaMalloc(&s->state, s->state_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        s->state = nullptr;
+        return fail(TG_ERR_OOM, "cudaMalloc of %zu state bytes failed", s->state_bytes);
+    }
+    if (cudaMalloc(&s->scratch, s->scratch_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        s->scratch = nullptr;
+        free_buffers(s);
+        return fail(TG_ERR_OOM, "cudaMalloc of %zu scratch bytes failed", s->scratch_bytes);
+    }
+    carve(s);
+    if (cudaMemset(s->state, 0, s->state_bytes) != cudaSuccess || cudaMemset(s->scratch, 0, s->scratch_bytes) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess) {
+        free_buffers(s);
+        return fail(TG_ERR_CUDA, "zeroing the SVGF state failed: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    return TG_OK;
+}
+
+int check_inputs(const tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* out)
+{
+    if (!in || !out) return fail(TG_ERR_INVALID, "null inputs or outputs");
+    static const int rad[] = {TG_FMT_RGBA32F, TG_FMT_RGBA16F};
+    static const int dep[] = {TG_FMT_R32F};
+    static const int nrm[] = {TG_FMT_RGB32F, TG_FMT_RGBA32F, TG_FMT_OCT16};
+    static const int mot[] = {TG_FMT_RG32F, TG_FMT_RG16F};
+    int st;
+    if ((st = check_image("radiance", in->radiance, s->w, s->h, rad, 2))) return st;
+    if ((st = check_image("denoised", out->denoised, s->w, s->h, rad, 2))) return st;
+    if (s->p.mode == TG_SVGF_MODE_FULL) {
+        if ((st = check_image("depth", in->depth, s->w, s->h, dep, 1))) return st;
+        if ((st = check_image("normal", in->normal, s->w, s->h, nrm, 3))) return st;
+        if ((st = check_image("motion", in->motion, s->w, s->h, mot, 2))) return st;
+    }
+    return TG_OK;
+}
+
+} // namespace
+
+namespace tg {
+
+static cudaEvent_t prof_event(tg_svgf* s)
+{
+    cudaEvent_t e = nullptr;
+    if (!s->prof.pool.empty()) {
+        e = s->prof.pool.back();
+        s->prof.pool.pop_back();
+    } else if (cudaEventCreate(&e) != cudaSuccess) {
+        e = nullptr;
+    }
+    return e;
+}
+
+// Launches `body` on `stream`, bracketed by an event pair when profiling.
+template <class F> static void launch(tg_svgf* s, cudaStream_t stream, int fam, double bytes, F body)
+{
+    if (!s->prof.on) {
+        body();
+        return;
+    }
+    cudaEvent_t a = prof_event(s), b = prof_event(s);
+    if (a) cudaEventRecord(a, stream);
+    body();
+    if (b) cudaEventRecord(b, stream);
+    if (a && b) {
+        s->prof.pending.push_back({fam, bytes, a, b});
+    } else {
+        if (a) s->prof.pool.push_back(a);
+        if (b) s->prof.pool.push_back(b);
+    }
+}
+
+// Enqueues one frame of the chain on `stream`.  Shared by the device and host
+// entry points.
+int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* out, cudaStream_t stream)
+{
+    const dim3 blk(kBlockX, kBlockY);
+    const dim3 grd((s->w + kBlockX - 1) / kBlockX, (s->h + kBlockY - 1) / kBlockY);
+    const int cur = int(s->frame & 1u), prev = cur ^ 1;
+    const bool f16 = s->p.storage == TG_SVGF_STORAGE_FP16;
+    if (s->p.mode == TG_SVGF_MODE_REF_EXACT) {
+        RefArgs a{};
+        a.w = int(s->w);
+        a.h = int(s->h);
+        a.raw = to_img(in->radiance, s->w);
+        a.out = to_img(out->denoised, s->w);
+        a.mom_prev = s->mom[prev];
+        a.mom_curr = s->mom[cur];
+        a.phi = s->p.sigma_l;
+        a.alpha_m = s->p.moments_alpha;
+        a.var_eps = s->p.variance_epsilon;
+        a.dst = s->colA;
+        const double npx = double(s->w) * s->h;
+        const double c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
+        const double rb = fmt_bytes(in->radiance.format), ob = fmt_bytes(out->denoised.format);
+        launch(s, stream, F_REF_INIT, npx * (rb + 2 * mm + c4), [&] {
+            if (f16)
+                k_ref_init<ST_FP16><<<grd, blk, 0, stream>>>(a);
+            else
+                k_ref_init<ST_FP32><<<grd, blk, 0, stream>>>(a);
+        });
+        void* src = s->colA;
+        void* oth = s->colB;
+        for (int lv = 0; lv < s->p.levels; ++lv) {
+            a.src = src;
+            a.dst = oth;
+            a.stride = 1 << lv;
+            a.final_pass = lv == s->p.levels - 1;
+            launch(s, stream, F_REF_LEVEL, npx * (c4 + (a.final_pass ? ob : c4)), [&] {
+                if (f16)
+                    k_ref_level<ST_FP16><<<grd, blk, 0, stream>>>(a);
+                else
+                    k_ref_level<ST_FP32><<<grd, blk, 0, stream>>>(a);
+            });
+            void* t = src;
+            src = oth;
+            oth = t;
+        }
+    } else {
+        FullArgs a{};
+        a.w = int(s->w);
+        a.h = int(s->h);
+        a.radiance = to_img(in->radiance, s->w);
+        a.depth = to_img(in->depth, s->w);
+        a.normal = to_img(in->normal, s->w);
+        a.motion = to_img(in->motion, s->w);
+        a.out = to_img(out->denoised, s->w);
+        a.guide_prev = s->guide[prev];
+        a.hist_prev = s->hist[prev];
+        a.mom_prev = s->mom[prev];
+        a.guide_cur = s->guide[cur];
+        a.hist_cur = s->hist[cur];
+        a.mom_cur = s->mom[cur];
+        a.tc = s->tc;
+        a.alpha = s->p.alpha;
+        a.alpha_m = s->p.moments_alpha;
+        a.sigma_l = s->p.sigma_l;
+        a.sigma_n = s->p.sigma_n;
+        a.sigma_z = s->p.sigma_z;
+        a.sq_n = sigma_n_squarings(s->p.sigma_n);
+        a.max_history = s->p.max_history;
+        a.fallback_frames = s->p.fallback_frames;
+        a.col_dst = s->colA;
+        const double npx = double(s->w) * s->h;
+        const double gb = f16 ? 8 : 16, c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
+        const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +
+                           fmt_bytes(in->normal.format) + fmt_bytes(in->motion.format);
+        const double ob = fmt_bytes(out->denoised.format);
+        // temporal: inputs + previous guide/history/moments, writes guide, tc, moments
+        launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm)), [&] {
+            if (f16)
+                k_full_temporal<ST_FP16><<<grd, blk, 0, stream>>>(a);
+            else
+                k_full_temporal<ST_FP32><<<grd, blk, 0, stream>>>(a);
+        });
+        // variance: tc + moments in, col out
+        launch(s, stream, F_FULL_VARIANCE, npx * (2 * c4 + mm), [&] {
+            if (f16)
+                k_full_variance<ST_FP16><<<grd, blk, 0, stream>>>(a);
+            else
+                k_full_variance<ST_FP32><<<grd, blk, 0, stream>>>(a);
+        });
+        void* src = s->colA;
+        void* oth = s->colB;
+        for (int lv = 0; lv < s->p.levels; ++lv) {
+            a.col_src = src;
+            a.col_dst = oth;
+            a.level = lv;
+            a.stride = 1 << lv;
+            a.last = lv == s->p.levels - 1;
+            // level: col + guide in, col (or output) out; level 0 also tc in, history out
+            const double lb = c4 + gb + (a.last ? ob : c4) + (lv == 0 ? 2 * c4 : 0);
+            launch(s, stream, F_FULL_LEVEL, npx * lb, [&] {
+                if (f16)
+                    k_full_level<ST_FP16><<<grd, blk, 0, stream>>>(a);
+                else
+                    k_full_level<ST_FP32><<<grd, blk, 0, stream>>>(a);
+            });
+            void* t = src;
+            src = oth;
+            oth = t;
+        }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TG_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    s->frame++;
+    return TG_OK;
+}
+
+} // namespace tg
+
+extern "C" {
+
+const char* tg_status_string(int status)
+{
+    switch (status) {
+    case TG_OK: return "ok";
+    case TG_ERR_INVALID: return "invalid argument";
+    case TG_ERR_OOM: return "out of memory";
+    case TG_ERR_CUDA: return "CUDA error";
+    case TG_ERR_TIMEOUT: return "timeout";
+    case TG_ERR_BUDGET: return "over HBM budget";
+    case TG_ERR_UNSUPPORTED: return "unsupported";
+    case TG_ERR_STATE: return "invalid state";
+    default: return "unknown status";
+    }
+}
+
+const char* tg_last_error(void) { return g_last_error.c_str(); }
+
+int tg_svgf_params_default(int32_t mode, int32_t storage, tg_svgf_params* out)
+{
+    if (!out) return fail(TG_ERR_INVALID, "null params");
+    if (mode != TG_SVGF_MODE_REF_EXACT && mode != TG_SVGF_MODE_FULL) return fail(TG_ERR_INVALID, "mode %d unknown", mode);
+    if (storage != TG_SVGF_STORAGE_FP32 && storage != TG_SVGF_STORAGE_FP16)
+        return fail(TG_ERR_INVALID, "storage %d unknown", storage);
+    std::memset(out, 0, sizeof *out);
+    out->mode = mode;
+    out->storage = storage;
+    if (mode == TG_SVGF_MODE_REF_EXACT) {
+        // src/svgf_denoise.slang:137 (SIGMA_COLOR_BASE), :144 (ALPHA_MOMENTS),
+        // :150 (VARIANCE_EPSILON); src/main.cpp:929 (three wavelet passes).
+        out->levels = 3;
+        out->sigma_l = 2.0f;
+        out->moments_alpha = 0.2f;
+        out->variance_epsilon = 1e-4f;
+        out->alpha = 1.0f;
+        out->max_history = 1;
+        out->fallback_frames = 0;
+        out->sigma_n = 1.0f;
+        out->sigma_z = 1.0f;
+    } else {
+        out->levels = 5;
+        out->alpha = 0.2f;
+        out->moments_alpha = 0.2f;
+        out->sigma_l = 4.0f;
+        out->sigma_n = 128.0f;
+        out->sigma_z = 1.0f;
+        out->max_history = 32;
+        out->fallback_frames = 4;
+        out->variance_epsilon = 1e-4f;
+    }
+    return TG_OK;
+}
+
+uint64_t tg_svgf_state_bytes(const tg_svgf_params* params, uint32_t width, uint32_t height)
+{
+    if (!params) return 0;
+    return state_bytes_of(*params, width, height);
+}
+
+int tg_svgf_create(const tg_svgf_desc* desc, tg_svgf** out)
+{
+    if (!desc || !out) return fail(TG_ERR_INVALID, "null descriptor or output handle");
+    *out = nullptr;
+    if (desc->width == 0 || desc->height == 0 || desc->width > 32768 || desc->height > 32768)
+        return fail(TG_ERR_INVALID, "size %ux%u outside 1..32768", desc->width, desc->height);
+    int st = validate_params(desc->params);
+    if (st) return st;
+    int dev = desc->device;
+    if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) return fail(TG_ERR_CUDA, "no current CUDA device");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || dev >= ndev) {
+        cudaGetLastError();
+        return fail(TG_ERR_CUDA, "CUDA device %d unavailable", dev);
+    }
+    DeviceGuard g(dev);
+    tg_svgf* s = new (std::nothrow) tg_svgf();
+    if (!s) return fail(TG_ERR_OOM, "host allocation failed");
+    s->device = dev;
+    s->w = desc->width;
+    s->h = desc->height;
+    s->p = desc->params;
+    st = alloc_buffers(s);
+    if (st) {
+        delete s;
+        return st;
+    }
+    *out = s;
+    return TG_OK;
+}
+
+int tg_svgf_denoise(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* out, void* stream)
+{
+    if (!s) return fail(TG_ERR_INVALID, "null handle");
+    int st = check_inputs(s, in, out);
+    if (st) return st;
+    DeviceGuard g(s->device);
+    return launch_frame(s, in, out, static_cast<cudaStream_t>(stream));
+}
+
+int tg_svgf_denoise_host(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* out, void* stream_v)
+{
+    if (!s) return fail(TG_ERR_INVALID, "null handle");
+    int st = check_inputs(s, in, out);
+    if (st) return st;
+    DeviceGuard g(s->device);
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+    const bool full = s->p.mode == TG_SVGF_MODE_FULL;
+    const tg_image* src_imgs[4] = {&in->radiance, &in->depth, &in->normal, &in->motion};
+    const int n_in = full ? 4 : 1;
+    size_t off[5], need = 0;
+    for (int k = 0; k < n_in; ++k) {
+        off[k] = need;
+        need += align_up(size_t(fmt_bytes(src_imgs[k]->format)) * s->w * s->h, 256);
+    }
+    off[4] = need;
+    need += align_up(size_t(fmt_bytes(out->denoised.format)) * s->w * s->h, 256);
+    if (!s->copy_stream && cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "copy stream creation failed");
+    tg_svgf::Staging& sg = s->stg[s->stg_next];
+    if (sg.bytes < need) {
+        if (sg.buf) {
+            // The previous use of this buffer must be finished before it is freed.
+            if (sg.used && cudaEventSynchronize(sg.ev_done) != cudaSuccess)
+                return fail(TG_ERR_CUDA, "staging wait failed");
+            cudaFree(sg.buf);
+            sg.buf = nullptr;
+            sg.bytes = 0;
+        }
+        if (cudaMalloc(&sg.buf, need) != cudaSuccess) {
+            cudaGetLastError();
+            sg.buf = nullptr;
+            return fail(TG_ERR_OOM, "cudaMalloc of %zu staging bytes failed", need);
+        }
+        sg.bytes = need;
+        sg.used = false;
+    }
+    if (!sg.ev_in) {
+        if (cudaEventCreateWithFlags(&sg.ev_in, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sg.ev_comp, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sg.ev_done, cudaEventDisableTiming) != cudaSuccess)
+            return fail(TG_ERR_CUDA, "event creation failed");
+    }
+    // H2D on the copy stream, after the previous user of this staging set has
+    // finished copying its result out.
+    if (sg.used && cudaStreamWaitEvent(s->copy_stream, sg.ev_done, 0) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "stream wait failed");
+    tg_svgf_inputs din{};
+    tg_image* dst_imgs[4] = {&din.radiance, &din.depth, &din.normal, &din.motion};
+    for (int k = 0; k < n_in; ++k) {
+        const tg_image& hi = *src_imgs[k];
+        const size_t row = size_t(fmt_bytes(hi.format)) * s->w;
+        const size_t hp = hi.pitch_bytes ? size_t(hi.pitch_bytes) : row;
+        *dst_imgs[k] = tg_image{sg.buf + off[k], int64_t(row), hi.format, 0};
+        if (cudaMemcpy2DAsync(sg.buf + off[k], row, hi.ptr, hp, row, s->h, cudaMemcpyHostToDevice, s->copy_stream) !=
+            cudaSuccess)
+            return fail(TG_ERR_CUDA, "input copy failed: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    if (cudaEventRecord(sg.ev_in, s->copy_stream) != cudaSuccess || cudaStreamWaitEvent(stream, sg.ev_in, 0) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "event record failed");
+    const size_t orow = size_t(fmt_bytes(out->denoised.format)) * s->w;
+    tg_svgf_outputs dout{};
+    dout.denoised = tg_image{sg.buf + off[4], int64_t(orow), out->denoised.format, 0};
+    st = launch_frame(s, &din, &dout, stream);
+    if (st) return st;
+    if (cudaEventRecord(sg.ev_comp, stream) != cudaSuccess || cudaStreamWaitEvent(s->copy_stream, sg.ev_comp, 0) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "event record failed");
+    const size_t op = out->denoised.pitch_bytes ? size_t(out->denoised.pitch_bytes) : orow;
+    if (cudaMemcpy2DAsync(out->denoised.ptr, op, sg.buf + off[4], orow, orow, s->h, cudaMemcpyDeviceToHost, s->copy_stream) !=
+        cudaSuccess)
+        return fail(TG_ERR_CUDA, "output copy failed: %s", cudaGetErrorString(cudaGetLastError()));
+    if (cudaEventRecord(sg.ev_done, s->copy_stream) != cudaSuccess) return fail(TG_ERR_CUDA, "event record failed");
+    sg.used = true;
+    s->stg_next ^= 1;
+    return TG_OK;
+}
+
+int tg_svgf_synchronize(tg_svgf* s)
+{
+    if (!s) return fail(TG_ERR_INVALID, "null handle");
+    DeviceGuard g(s->device);
+    for (auto& sg : s->stg)
+        if (sg.used && cudaEventSynchronize(sg.ev_done) != cudaSuccess)
+            return fail(TG_ERR_CUDA, "synchronize failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return TG_OK;
+}
+
+int tg_svgf_reset(tg_svgf* s, void* stream)
+{
+    if (!s) return fail(TG_ERR_INVALID, "null handle");
+    DeviceGuard g(s->device);
+    if (cudaMemsetAsync(s->state, 0, s->state_bytes, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "reset failed: %s", cudaGetErrorString(cudaGetLastError()));
+    s->frame = 0;
+    return TG_OK;
+}
+
+int tg_svgf_resize(tg_svgf* s, uint32_t width, uint32_t height)
+{
+    if (!s) return fail(TG_ERR_INVALID, "null handle");
+    if (width == 0 || height == 0 || width > 32768 || height > 32768)
+        return fail(TG_ERR_INVALID, "size %ux%u outside 1..32768", width, height);
+    DeviceGuard g(s->device);
+    if (cudaDeviceSynchronize() != cudaSuccess) return fail(TG_ERR_CUDA, "synchronize failed");
+    free_buffers(s);
+    free_staging(s);
+    s->w = width;
+    s->h = height;
+    s->frame = 0;
+    return alloc_buffers(s);
+}
+
+int tg_svgf_get_info(const tg_svgf* s, tg_svgf_info* info)
+{
+    if (!s || !info) return fail(TG_ERR_INVALID, "null handle or info");
+    std::memset(info, 0, sizeof *info);
+    info->width = s->w;
+    info->height = s->h;
+    info->frame_index = s->frame;
+    info->state_bytes = s->state_bytes;
+    info->scratch_bytes = s->scratch_bytes;
+    info->staging_bytes = s->stg[0].bytes + s->stg[1].bytes;
+    info->kernels_per_frame = uint32_t(s->p.levels + (s->p.mode == TG_SVGF_MODE_FULL ? 2 : 1));
+    return TG_OK;
+}
+
+int tg_svgf_profile_enable(tg_svgf* s, int enable)
+{
+    if (!s) return fail(TG_ERR_INVALID, "null handle");
+    s->prof.on = enable != 0;
+    return TG_OK;
+}
+
+int tg_svgf_profile_read(tg_svgf* s, tg_svgf_kernel_stat* stats, int capacity, int* count, int reset)
+{
+    if (!s || !count || (capacity > 0 && !stats)) return fail(TG_ERR_INVALID, "null argument");
+    DeviceGuard g(s->device);
+    for (auto& r : s->prof.pending) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess)
+            return fail(TG_ERR_CUDA, "profile event failed: %s", cudaGetErrorString(cudaGetLastError()));
+        s->prof.launches[r.fam] += 1;
+        s->prof.ms[r.fam] += ms;
+        s->prof.bytes[r.fam] += r.bytes;
+        s->prof.pool.push_back(r.a);
+        s->prof.pool.push_back(r.b);
+    }
+    s->prof.pending.clear();
+    int n = 0;
+    for (int f = 0; f < kFamilies; ++f) {
+        if (!s->prof.launches[f]) continue;
+        if (n < capacity) {
+            tg_svgf_kernel_stat& o = stats[n];
+            std::memset(&o, 0, sizeof o);
+            std::snprintf(o.name, sizeof o.name, "%s", kFamilyName[f]);
+            o.launches = s->prof.launches[f];
+            o.total_ms = s->prof.ms[f];
+            o.algo_bytes = s->prof.bytes[f];
+        }
+        ++n;
+    }
+    *count = n;
+    if (reset) {
+        for (int f = 0; f < kFamilies; ++f) {
+            s->prof.launches[f] = 0;
+            s->prof.ms[f] = 0.0;
+            s->prof.bytes[f] = 0.0;
+        }
+    }
+    return TG_OK;
+}
+
+void tg_svgf_destroy(tg_svgf* s)
+{
+    if (!s) return;
+    DeviceGuard g(s->device);
+    cudaDeviceSynchronize();
+    for (auto& r : s->prof.pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : s->prof.pool) cudaEventDestroy(e);
+    free_staging(s);
+    free_buffers(s);
+    delete s;
+}
+
+} // extern "C"

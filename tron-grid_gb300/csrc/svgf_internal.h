@@ -1,0 +1,29 @@
+// Helpers shared by the translation units of the SVGF library (not part of
+// the public ABI).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "tg_svgf.h"
+
+struct tg_svgf;
+
+namespace tg {
+
+struct Img;
+
+extern thread_local std::string g_last_error;
+
+// Records a message for tg_last_error() and returns `status`.
+int fail(int status, const char* fmt, ...);
+
+int fmt_bytes(int fmt);
+int check_image(const char* what, const tg_image& im, uint32_t w, uint32_t h, const int* allowed, int n_allowed);
+int validate_params(const tg_svgf_params& p);
+int sigma_n_squarings(float sigma_n);
+size_t state_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
+size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
+
+} // namespace tg
