@@ -17,6 +17,7 @@
 
 #include "svgf_internal.h"
 #include "svgf_kernels.cuh"
+#include "svgf_level.cuh"
 
 using namespace tg;
 
@@ -117,12 +118,26 @@ size_t state_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
     return 2 * (align_up(n * l.guide, 256) + align_up(n * l.c4, 256) + align_up(n * l.mom, 256));
 }
 
+// Pixels of one a-trous scratch buffer: the largest residue-major layout any
+// level reads or writes (strides 1 .. 2^(levels-1)).
+static size_t col_pixels(const tg_svgf_params& p, uint32_t w, uint32_t h)
+{
+    size_t n = 0;
+    for (int lg = 0; lg < p.levels; ++lg) {
+        const size_t s = size_t(1) << lg;
+        const size_t m = s * s * ((w + s - 1) / s) * ((h + s - 1) / s);
+        n = m > n ? m : n;
+    }
+    return n;
+}
+
 size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     const size_t n = size_t(w) * h;
     const Layout l = layout_of(p);
-    if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * align_up(n * l.c4, 256);
-    return 3 * align_up(n * l.c4, 256);
+    const size_t col = align_up(col_pixels(p, w, h) * l.c4, 256);
+    if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * col;
+    return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256);
 }
 
 int validate_params(const tg_svgf_params& p)
@@ -169,6 +184,7 @@ struct tg_svgf {
     void* tc = nullptr;
     void* colA = nullptr;
     void* colB = nullptr;
+    float2* grad = nullptr;
     // host-call staging (double buffered)
     struct Staging {
         char* buf = nullptr;
@@ -223,9 +239,10 @@ void carve(tg_svgf* s)
         s->mom[0] = take(n * l.mom);
         s->mom[1] = take(n * l.mom);
         p = s->scratch;
-        s->colA = take(n * l.c4);
-        s->colB = take(n * l.c4);
+        s->colA = take(col_pixels(s->p, s->w, s->h) * l.c4);
+        s->colB = take(col_pixels(s->p, s->w, s->h) * l.c4);
         s->guide[0] = s->guide[1] = s->hist[0] = s->hist[1] = s->tc = nullptr;
+        s->grad = nullptr;
     } else {
         for (int k = 0; k < 2; ++k) {
             s->guide[k] = take(n * l.guide);
@@ -234,8 +251,9 @@ void carve(tg_svgf* s)
         }
         p = s->scratch;
         s->tc = take(n * l.c4);
-        s->colA = take(n * l.c4);
-        s->colB = take(n * l.c4);
+        s->colA = take(col_pixels(s->p, s->w, s->h) * l.c4);
+        s->colB = take(col_pixels(s->p, s->w, s->h) * l.c4);
+        s->grad = static_cast<float2*>(take(n * sizeof(float2)));
     }
 }
 
@@ -306,6 +324,9 @@ int check_inputs(const tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outpu
 
 namespace tg {
 
+// Output rows per thread of the tiled a-trous kernels.
+constexpr int kLevelR = 2;
+
 static cudaEvent_t prof_event(tg_svgf* s)
 {
     cudaEvent_t e = nullptr;
@@ -373,11 +394,15 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             a.dst = oth;
             a.stride = 1 << lv;
             a.final_pass = lv == s->p.levels - 1;
+            a.lin = res_layout(a.w, a.h, lv);
+            a.lout = res_layout(a.w, a.h, lv + 1);
+            const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
+            const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
             launch(s, stream, F_REF_LEVEL, npx * (c4 + (a.final_pass ? ob : c4)), [&] {
                 if (f16)
-                    k_ref_level<ST_FP16><<<grd, blk, 0, stream>>>(a);
+                    k_ref_level_tiled<ST_FP16, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
                 else
-                    k_ref_level<ST_FP32><<<grd, blk, 0, stream>>>(a);
+                    k_ref_level_tiled<ST_FP32, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
             });
             void* t = src;
             src = oth;
@@ -399,6 +424,7 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.hist_cur = s->hist[cur];
         a.mom_cur = s->mom[cur];
         a.tc = s->tc;
+        a.grad = s->grad;
         a.alpha = s->p.alpha;
         a.alpha_m = s->p.moments_alpha;
         a.sigma_l = s->p.sigma_l;
@@ -435,13 +461,17 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             a.level = lv;
             a.stride = 1 << lv;
             a.last = lv == s->p.levels - 1;
+            a.lin = res_layout(a.w, a.h, lv);
+            a.lout = res_layout(a.w, a.h, lv + 1);
             // level: col + guide in, col (or output) out; level 0 also tc in, history out
             const double lb = c4 + gb + (a.last ? ob : c4) + (lv == 0 ? 2 * c4 : 0);
+            const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
+            const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
             launch(s, stream, F_FULL_LEVEL, npx * lb, [&] {
                 if (f16)
-                    k_full_level<ST_FP16><<<grd, blk, 0, stream>>>(a);
+                    k_full_level_tiled<ST_FP16, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
                 else
-                    k_full_level<ST_FP32><<<grd, blk, 0, stream>>>(a);
+                    k_full_level_tiled<ST_FP32, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
             });
             void* t = src;
             src = oth;

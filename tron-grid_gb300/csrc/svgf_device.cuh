@@ -32,6 +32,35 @@ constexpr float kDepthGrad = 4.0f; // reprojection depth test: gradient term
 constexpr float kDepthAbs = 0.1f;  // reprojection depth test: absolute term
 constexpr float kNormalCos = 0.9f; // reprojection normal test: minimum cosine
 constexpr float kHalfMax = 65504.0f;
+constexpr float kLog2eF = 1.4426950408889634f;
+
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float lg2_approx(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 __device__ __forceinline__ float b3(int i)
 {

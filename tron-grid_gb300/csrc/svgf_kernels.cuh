@@ -13,6 +13,31 @@ namespace tg {
 constexpr int kBlockX = 32;
 constexpr int kBlockY = 8;
 
+// Residue-major layout of the a-trous scratch for stride s = 2^lg: pixel
+// (x, y) lives in plane (y mod s) * s + (x mod s) at position (x / s, y / s),
+// each plane pw x ph.  For s = 1 this is the ordinary row-major image.  Level
+// L reads its input in the layout of its own stride and writes its output in
+// the layout of the next level's stride, so every tile a level stages and
+// every 3x3 neighbourhood it reads is a contiguous run of memory.
+struct ResLayout {
+    int lg, pw, ph;
+};
+
+__device__ __forceinline__ size_t res_idx(const ResLayout& L, int x, int y)
+{
+    const int m = (1 << L.lg) - 1;
+    return (size_t(((y & m) << L.lg) + (x & m)) * L.ph + (y >> L.lg)) * L.pw + (x >> L.lg);
+}
+
+inline ResLayout res_layout(int w, int h, int lg)
+{
+    ResLayout L;
+    L.lg = lg;
+    L.pw = (w + (1 << lg) - 1) >> lg;
+    L.ph = (h + (1 << lg) - 1) >> lg;
+    return L;
+}
+
 // ------------------------------------------------------------- REF-EXACT ----
 // src/svgf_denoise.slang:152-275, one kernel per pass.
 
@@ -24,6 +49,7 @@ struct RefArgs {
     void* mom_curr;       // moments_curr (b5)
     const void* src;      // wavelet source (b1 or b2)
     void* dst;            // wavelet destination (b2 or b1)
+    ResLayout lin, lout;  // scratch layouts of src and dst
     float phi;            // SIGMA_COLOR_BASE
     float alpha_m;        // ALPHA_MOMENTS
     float var_eps;        // VARIANCE_EPSILON
@@ -56,54 +82,6 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_ref_init
     S::st4(static_cast<typename S::c4_t*>(a.dst), i, make_float4(c.x, c.y, c.z, sd));
 }
 
-// Passes 1..3 (src/svgf_denoise.slang:209-274): 5x5 B3 taps at `stride`,
-// clamp-to-edge, luminance edge stop exp(-|dl| / max(phi * sqrt_var, eps)).
-template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_ref_level(RefArgs a)
-{
-    typedef Stor<ST> S;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    if (x >= a.w || y >= a.h) return;
-    const typename S::c4_t* src = static_cast<const typename S::c4_t*>(a.src);
-    const size_t i = size_t(y) * a.w + x;
-    const float4 c = S::ld4(src, i);
-    const float cl = lum(c.x, c.y, c.z);
-    const float sigma = fmaxf(__fmul_rn(a.phi, c.w), a.var_eps);
-    const float nis = -1.0f / sigma;
-    const int mx = a.w - 1, my = a.h - 1, s = a.stride;
-    float sr = 0.0f, sg = 0.0f, sb = 0.0f, ws = 0.0f;
-#pragma unroll
-    for (int dy = -2; dy <= 2; ++dy) {
-        const int sy = min(max(y + dy * s, 0), my);
-        const size_t row = size_t(sy) * a.w;
-#pragma unroll
-        for (int dx = -2; dx <= 2; ++dx) {
-            const int sx = min(max(x + dx * s, 0), mx);
-            const float4 q = S::ld4(src, row + sx);
-            const float ql = lum(q.x, q.y, q.z);
-            const float kw = b3(dx + 2) * b3(dy + 2);
-            const float tw = kw * __expf(fabsf(ql - cl) * nis);
-            sr = fmaf(q.x, tw, sr);
-            sg = fmaf(q.y, tw, sg);
-            sb = fmaf(q.z, tw, sb);
-            ws += tw;
-        }
-    }
-    float4 o;
-    if (ws > 1e-6f) {
-        o = make_float4(__fdiv_rn(sr, ws), __fdiv_rn(sg, ws), __fdiv_rn(sb, ws), c.w);
-    } else {
-        o = make_float4(c.x, c.y, c.z, c.w);
-    }
-    if (a.final_pass) {
-        o.w = 1.0f;
-        if (ST == ST_FP16) o = make_float4(q16(o.x), q16(o.y), q16(o.z), 1.0f);
-        st_rgba(a.out, x, y, o);
-    } else {
-        S::st4(static_cast<typename S::c4_t*>(a.dst), i, o);
-    }
-}
-
 // ------------------------------------------------------------------ FULL ----
 
 struct FullArgs {
@@ -118,28 +96,13 @@ struct FullArgs {
     void* tc;
     const void* col_src;
     void* col_dst;
+    float2* grad;           // per-pixel depth gradient (written by the temporal kernel)
+    ResLayout lin, lout;    // scratch layouts of col_src and col_dst
     float alpha, alpha_m, sigma_l, sigma_n, sigma_z;
     int sq_n; // squarings for sigma_n = 2^sq_n, -1 otherwise
     int max_history, fallback_frames;
     int level, stride, last;
 };
-
-template <int ST> __device__ __forceinline__ float guide_z(const FullArgs& a, int x, int y)
-{
-    return Stor<ST>::ld_guide_z(static_cast<const typename Stor<ST>::guide_t*>(a.guide_cur), size_t(y) * a.w + x);
-}
-
-template <int ST> __device__ __forceinline__ void guide_grad(const FullArgs& a, int x, int y, float z, float& gx,
-                                                             float& gy)
-{
-    const bool hl = x > 0, hr = x < a.w - 1, hu = y > 0, hd = y < a.h - 1;
-    float zl = hl ? guide_z<ST>(a, x - 1, y) : 0.0f;
-    float zr = hr ? guide_z<ST>(a, x + 1, y) : 0.0f;
-    float zu = hu ? guide_z<ST>(a, x, y - 1) : 0.0f;
-    float zd = hd ? guide_z<ST>(a, x, y + 1) : 0.0f;
-    gx = grad1(z, zl, zr, hl, hr);
-    gy = grad1(z, zu, zd, hu, hd);
-}
 
 // K1: guide write, reprojection (bilinear 2x2 with depth/normal test), history
 // length, colour EMA and mean-centred moment EMA.
@@ -164,6 +127,7 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_tem
     const float gx = grad1(z, hl ? ld_depth(a.depth, x - 1, y) : 0.0f, hr ? ld_depth(a.depth, x + 1, y) : 0.0f, hl, hr);
     const float gy = grad1(z, hu ? ld_depth(a.depth, x, y - 1) : 0.0f, hd ? ld_depth(a.depth, x, y + 1) : 0.0f, hu, hd);
 
+    a.grad[i] = make_float2(gx, gy);
     const float4 c4 = ld_rgba(a.radiance, x, y);
     const float cr = S::qin(c4.x), cg = S::qin(c4.y), cb = S::qin(c4.z);
     const float gsum = __fadd_rn(fabsf(gx), fabsf(gy));
@@ -269,28 +233,29 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_var
     float var = mom.y;
     if (len < a.fallback_frames) {
         const float4 g = S::ld_guide(gc, i);
-        float gx, gy;
-        guide_grad<ST>(a, x, y, g.w, gx, gy);
+        const float2 gr = a.grad[i];
+        // w = max(0, n.n')^sigma_n exp(-|dz| / (sigma_z |grad z . off| + eps_z)), as one ex2
+        const float A_ = a.sigma_z * gr.x * (1.0f / kLog2eF), B_ = a.sigma_z * gr.y * (1.0f / kLog2eF);
+        const float ez = kEpsZ * (1.0f / kLog2eF);
         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
         for (int dy = -3; dy <= 3; ++dy) {
             const int qy = y + dy;
             if (qy < 0 || qy >= a.h) continue;
+#pragma unroll
             for (int dx = -3; dx <= 3; ++dx) {
                 const int qx = x + dx;
                 if (qx < 0 || qx >= a.w) continue;
                 const size_t j = size_t(qy) * a.w + qx;
                 const float4 q = S::ld_guide(gc, j);
-                const float d = dot3_rn(q.x, q.y, q.z, g.x, g.y, g.z);
-                const float wn = normal_weight(d, a.sq_n, a.sigma_n);
-                if (!(wn > 0.0f)) continue;
-                const float den = a.sigma_z * fabsf(float(dx) * gx + float(dy) * gy) + kEpsZ;
-                const float ez = fabsf(q.w - g.w) / den;
-                const float wgt = wn * __expf(-ez);
+                const float d = fmaf(q.z, g.z, fmaf(q.y, g.y, q.x * g.x));
+                float t = -fabsf(q.w - g.w) * rcp_approx(fabsf(float(dx) * A_ + float(dy) * B_) + ez);
+                t = fmaf(a.sigma_n, lg2_approx(fmaxf(d, 0.0f)), t);
+                const float wgt = ex2_approx(t);
                 const float2 m = S::ldm(mc, j);
                 const float dm = m.x - mom.x;
                 s0 += wgt;
-                s1 += wgt * dm;
-                s2 += wgt * (dm * dm + m.y);
+                s1 = fmaf(wgt, dm, s1);
+                s2 = fmaf(wgt, fmaf(dm, dm, m.y), s2);
             }
         }
         if (s0 > 0.0f) {
@@ -299,90 +264,6 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_var
         }
     }
     S::st4_sat_w(static_cast<C4*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var));
-}
-
-// K3: one a-trous level at stride 2^level.  Edge stops: luminance
-// exp(-|dl| / (sigma_l sqrt(g3x3 var) + eps)), normal max(0, n.n')^sigma_n,
-// depth exp(-|dz| / (sigma_z |grad z . offset| + eps)).  Taps outside the image
-// are skipped.  Variance is propagated with squared weights.  Level 0 writes
-// the colour history; the last level writes the caller's output.
-template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_level(FullArgs a)
-{
-    typedef Stor<ST> S;
-    typedef typename S::guide_t G;
-    typedef typename S::c4_t C4;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    if (x >= a.w || y >= a.h) return;
-    const size_t i = size_t(y) * a.w + x;
-    const C4* src = static_cast<const C4*>(a.col_src);
-    const G* gc = static_cast<const G*>(a.guide_cur);
-    const float4 c = S::ld4(src, i);
-    const float cl = lum(c.x, c.y, c.z);
-    const float4 g = S::ld_guide(gc, i);
-    float gx, gy;
-    guide_grad<ST>(a, x, y, g.w, gx, gy);
-
-    float gv = 0.0f, gw = 0.0f;
-#pragma unroll
-    for (int dy = -1; dy <= 1; ++dy) {
-        const int qy = y + dy;
-        if (qy < 0 || qy >= a.h) continue;
-#pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
-            const int qx = x + dx;
-            if (qx < 0 || qx >= a.w) continue;
-            const float k = (dy == 0 ? 0.5f : 0.25f) * (dx == 0 ? 0.5f : 0.25f);
-            gv += k * S::ld4_w(src, size_t(qy) * a.w + qx);
-            gw += k;
-        }
-    }
-    gv = __fdiv_rn(gv, gw);
-    const float inv_l = 1.0f / (a.sigma_l * sqrtf(fmaxf(gv, 0.0f)) + kEpsL);
-    const int s = a.stride;
-    float sr = 0.0f, sg = 0.0f, sb = 0.0f, sw = 0.0f, sv = 0.0f;
-#pragma unroll
-    for (int dy = -2; dy <= 2; ++dy) {
-        const int qy = y + dy * s;
-        if (qy < 0 || qy >= a.h) continue;
-#pragma unroll
-        for (int dx = -2; dx <= 2; ++dx) {
-            const int qx = x + dx * s;
-            if (qx < 0 || qx >= a.w) continue;
-            const size_t j = size_t(qy) * a.w + qx;
-            const float4 q = S::ld_guide(gc, j);
-            const float d = dot3_rn(q.x, q.y, q.z, g.x, g.y, g.z);
-            const float wn = normal_weight(d, a.sq_n, a.sigma_n);
-            if (!(wn > 0.0f)) continue;
-            const float4 v = S::ld4(src, j);
-            const float ql = lum(v.x, v.y, v.z);
-            const float el = fabsf(cl - ql) * inv_l;
-            const float den = a.sigma_z * fabsf(float(s) * (float(dx) * gx + float(dy) * gy)) + kEpsZ;
-            const float ez = __fdividef(fabsf(g.w - q.w), den);
-            const float wgt = b3(dx + 2) * b3(dy + 2) * wn * __expf(-(el + ez));
-            sr = fmaf(wgt, v.x, sr);
-            sg = fmaf(wgt, v.y, sg);
-            sb = fmaf(wgt, v.z, sb);
-            sw += wgt;
-            sv = fmaf(wgt * wgt, v.w, sv);
-        }
-    }
-    float4 o;
-    if (sw > 0.0f) {
-        const float inv = 1.0f / sw;
-        o = make_float4(sr * inv, sg * inv, sb * inv, sv * (inv * inv));
-    } else {
-        o = c;
-    }
-    if (a.level == 0) {
-        const float len = S::ld4_w(static_cast<const C4*>(a.tc), i);
-        S::st4(static_cast<C4*>(a.hist_cur), i, make_float4(o.x, o.y, o.z, len));
-    }
-    if (a.last) {
-        st_rgba(a.out, x, y, make_float4(S::qin(o.x), S::qin(o.y), S::qin(o.z), 1.0f));
-    } else {
-        S::st4_sat_w(static_cast<C4*>(a.col_dst), i, o);
-    }
 }
 
 } // namespace tg
