@@ -83,3 +83,16 @@ def test_missing_library_fails_loudly(tmp_path):
             L.load(str(tmp_path / "nope.so"))
         finally:
             L._lib = L._lib_backup
+
+
+def test_cpp_wrapper_compiles(tmp_path):
+    import shutil
+    import subprocess
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    src = tmp_path / "use.cpp"
+    src.write_text('#include "tg_svgf.hpp"\nint main() { try { tg::SvgfDenoiser d(16, 16); } catch (const tg::Error&) {} }\n')
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
