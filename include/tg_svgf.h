@@ -207,6 +207,33 @@ typedef struct tg_svgf_kernel_stat {
 TG_API int tg_svgf_profile_enable(tg_svgf* h, int enable);
 TG_API int tg_svgf_profile_read(tg_svgf* h, tg_svgf_kernel_stat* stats, int capacity, int* count, int reset);
 
+/* Reference-exact frame for callers that cannot allocate device memory.
+ * This entry point has no counterpart in the reference.  It exists for callers
+ * that must not call cudaMalloc while they denoise: a real-time render thread
+ * (a device allocation can stall for milliseconds and may synchronise the
+ * device mid-frame) and plug-in hosts that give their plug-ins a fixed memory
+ * budget or only buffers and streams they already own.  Such callers cannot
+ * create a tg_svgf handle, which allocates its state.
+ *
+ * The caller passes every image: radiance in, moments_prev in, moments_curr
+ * out (the reference's moments ping-pong, src/svgf_denoise.slang:76-82:
+ * RG16F with TG_SVGF_STORAGE_FP16, RG32F with TG_SVGF_STORAGE_FP32, tightly
+ * packed, zero for the first frame) and denoised out.  The only scratch, the
+ * two wavelet ping-pong images, lives in a fixed 16 MiB device array inside
+ * this library, which every GPU that loads the library holds until exit.
+ * That bounds the frame to about 1 Mpx with fp16 images (e.g. 1280x720) and
+ * about 0.5 Mpx with fp32 images (e.g. 960x540); larger frames are rejected
+ * with TG_ERR_INVALID.  params->mode must be TG_SVGF_MODE_REF_EXACT.
+ *
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the array, so calls whose work overlaps on the GPU
+ * race: serialise them (for example on one stream).  No call allocates. */
+#define TG_SVGF_NOALLOC_SCRATCH_BYTES (16u << 20)
+TG_API int tg_svgf_denoise_ref_noalloc(const tg_svgf_params* params, uint32_t width, uint32_t height,
+                                       const tg_image* radiance, const tg_image* moments_prev,
+                                       const tg_image* moments_curr, const tg_image* denoised, void* stream);
+
 /* Bytes of device state a FULL or REF_EXACT stream of w x h keeps resident
  * (history, moments, guide), for admission control. */
 TG_API uint64_t tg_svgf_state_bytes(const tg_svgf_params* params, uint32_t width, uint32_t height);

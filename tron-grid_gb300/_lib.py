@@ -81,6 +81,8 @@ SIGNATURES = {
     "tg_svgf_state_bytes": (C.c_uint64, [C.POINTER(Params), C.c_uint32, C.c_uint32]),
     "tg_svgf_profile_enable": (C.c_int, [_P, C.c_int]),
     "tg_svgf_profile_read": (C.c_int, [_P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int), C.c_int]),
+    "tg_svgf_denoise_ref_noalloc": (C.c_int, [C.POINTER(Params), C.c_uint32, C.c_uint32, C.POINTER(Image),
+                                              C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), _P]),
 }
 
 _lib = None
