@@ -207,6 +207,69 @@ typedef struct tg_svgf_kernel_stat {
 TG_API int tg_svgf_profile_enable(tg_svgf* h, int enable);
 TG_API int tg_svgf_profile_read(tg_svgf* h, tg_svgf_kernel_stat* stats, int capacity, int* count, int reset);
 
+/* ---------------------------------------------------------------- batches --
+ * Many independent camera streams of uneven resolution (the bot-mode eye
+ * frames of docs/AI_INTERFACE.md:340-380, which the reference only designs)
+ * denoised together: every frame step of the listed streams runs as ONE
+ * persistent cooperative launch that walks a tile work-list spanning all
+ * streams, stage by stage (temporal, variance, a-trous levels) with a bounded
+ * grid barrier between stages, optionally replayed from a CUDA graph.  FULL
+ * mode only.  Each stream keeps its own history/moments/guide state on the
+ * device; a stream's result is identical alone and in any mix of streams. */
+#define TG_SVGF_BATCH_MAX_STREAMS 1024
+
+typedef struct tg_svgf_batch tg_svgf_batch;
+
+typedef struct tg_svgf_batch_desc {
+    uint32_t n_streams;        /* 1 .. TG_SVGF_BATCH_MAX_STREAMS */
+    const uint32_t* widths;    /* n_streams widths */
+    const uint32_t* heights;   /* n_streams heights */
+    tg_svgf_params params;     /* mode must be TG_SVGF_MODE_FULL */
+    int32_t device;            /* -1 = current */
+    int32_t rows_per_thread;   /* a-trous outputs per thread (tile 32 x 8r): 1 or 2; 0 = 2 until autotuned */
+    int32_t ctas_per_sm;       /* persistent CTAs per SM: 1..3; 0 = the occupancy limit */
+    int32_t use_graph;         /* nonzero: replay each step from a captured CUDA graph */
+} tg_svgf_batch_desc;
+
+typedef struct tg_svgf_batch_info {
+    uint32_t n_streams;
+    int32_t rows_per_thread;   /* current tile shape: 32 x (8 * rows_per_thread) outputs */
+    int32_t ctas_per_sm;
+    int32_t grid_ctas;         /* persistent grid size */
+    int32_t graphs;            /* 1 when steps replay CUDA graphs */
+    int32_t reserved;
+    uint64_t state_bytes;      /* device state of all streams */
+    uint64_t scratch_bytes;    /* device scratch of all streams */
+    uint64_t steps;            /* frame steps run */
+    uint64_t barrier_timeouts; /* steps whose grid barrier gave up (TG_ERR_TIMEOUT) */
+    double tuned_ms;           /* step time of the autotuned choice (0 before tuning) */
+} tg_svgf_batch_info;
+
+TG_API int tg_svgf_batch_create(const tg_svgf_batch_desc* desc, tg_svgf_batch** out);
+
+/* One frame step: stream_ids[k] gets inputs[k] and writes outputs[k]
+ * (device images, FULL-mode formats).  A stream may appear at most once.
+ * Enqueued on `stream`; reports TG_ERR_TIMEOUT for an earlier step whose grid
+ * barrier gave up (that step's outputs are invalid). */
+TG_API int tg_svgf_batch_denoise(tg_svgf_batch* b, uint32_t n, const uint32_t* stream_ids,
+                                 const tg_svgf_inputs* inputs, const tg_svgf_outputs* outputs, void* stream);
+
+/* Times every (rows_per_thread, ctas_per_sm) candidate on `steps` steps of the
+ * given frames, keeps the fastest, then zeroes every stream's state. */
+TG_API int tg_svgf_batch_autotune(tg_svgf_batch* b, uint32_t n, const uint32_t* stream_ids,
+                                  const tg_svgf_inputs* inputs, const tg_svgf_outputs* outputs, uint32_t steps,
+                                  void* stream);
+
+/* Zeroes one stream's history (its next frame is a full disocclusion). */
+TG_API int tg_svgf_batch_reset_stream(tg_svgf_batch* b, uint32_t stream_id, void* stream);
+
+/* Waits for the batch's work and reports a barrier timeout of any step. */
+TG_API int tg_svgf_batch_synchronize(tg_svgf_batch* b);
+
+TG_API int tg_svgf_batch_get_info(const tg_svgf_batch* b, tg_svgf_batch_info* info);
+
+TG_API void tg_svgf_batch_destroy(tg_svgf_batch* b);
+
 /* Reference-exact frame for callers that cannot allocate device memory.
  * This entry point has no counterpart in the reference.  It exists for callers
  * that must not call cudaMalloc while they denoise: a real-time render thread

@@ -1,0 +1,143 @@
+"""The batched form: one persistent launch per step over many streams.
+
+Each stream's output must equal (bit for bit) what the single-stream path
+computes for the same frames - alone and in any mix of streams - and, for the
+FP16 form, stay within the parity bounds against the oracle.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import tron_grid_gb300 as tg
+from tron_grid_gb300 import scene
+from tron_grid_gb300.batch import Batch
+from tests.helpers import rel_err, rel_l2
+
+pytestmark = pytest.mark.gpu
+KEYS = ("radiance", "depth", "normal", "motion")
+SIZES = [(17, 9), (64, 36), (160, 90), (33, 17), (96, 64), (1, 1)]
+
+
+def _streams(sizes, frames, dev, f16=False, seed=0):
+    specs = [scene.config1(w, h, seed=seed + 13 * k) for k, (w, h) in enumerate(sizes)]
+    out = []
+    for sp in specs:
+        sc = scene.PlaneScene(sp)
+        seq = []
+        for t in range(frames):
+            fr = sc.frame(t)
+            d = {k: fr[k].to(dev) for k in KEYS}
+            if f16:
+                d["radiance"] = d["radiance"].half()
+                d["normal"] = torch.from_numpy(oracle.oct16_encode(fr["normal"].numpy())).to(dev)
+            seq.append(d)
+        out.append(seq)
+    return out
+
+
+def _single(sizes, seqs, storage, dev):
+    res = []
+    for (w, h), seq in zip(sizes, seqs):
+        d = tg.Denoiser(w, h, storage=storage)
+        dt = torch.float16 if storage == tg.STORAGE_FP16 else torch.float32
+        outs = []
+        for fr in seq:
+            o = torch.empty((h, w, 4), dtype=dt, device=dev)
+            d.denoise(fr["radiance"], fr["depth"], fr["normal"], fr["motion"], out=o)
+            outs.append(o.cpu())
+        d.close()
+        res.append(outs)
+    return res
+
+
+@pytest.mark.parametrize("storage", [tg.STORAGE_FP32, tg.STORAGE_FP16])
+@pytest.mark.parametrize("rows", [1, 2])
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_equals_single_stream(cuda_dev, storage, rows, graph):
+    f16 = storage == tg.STORAGE_FP16
+    frames = 5
+    seqs = _streams(SIZES, frames, cuda_dev, f16=f16)
+    want = _single(SIZES, seqs, storage, cuda_dev)
+    b = Batch(SIZES, storage=storage, rows_per_thread=rows, use_graph=graph)
+    dt = torch.float16 if f16 else torch.float32
+    ids = list(range(len(SIZES)))
+    for t in range(frames):
+        outs = [torch.empty((h, w, 4), dtype=dt, device=cuda_dev) for (w, h) in SIZES]
+        b.denoise(ids, [seqs[j][t] for j in ids], outs)
+        b.synchronize()
+        for j in ids:
+            assert torch.equal(outs[j].cpu(), want[j][t]), f"stream {j} frame {t}"
+    info = b.info()
+    assert info["steps"] == frames and info["barrier_timeouts"] == 0
+    b.close()
+
+
+def test_alone_equals_in_mix_with_subsets(cuda_dev):
+    """A stream's results are the same whether it runs alone or with others, including partial steps."""
+    frames = 4
+    seqs = _streams(SIZES, frames, cuda_dev)
+    alone = Batch(SIZES[2:3], storage=tg.STORAGE_FP32)
+    mix = Batch(SIZES, storage=tg.STORAGE_FP32)
+    for t in range(frames):
+        oa = [torch.empty((90, 160, 4), device=cuda_dev)]
+        alone.denoise([0], [seqs[2][t]], oa)
+        # the mix advances stream 2 every step, the others only on even steps
+        ids = [2] + ([0, 1, 3, 4, 5] if t % 2 == 0 else [4])
+        om = [torch.empty((SIZES[j][1], SIZES[j][0], 4), device=cuda_dev) for j in ids]
+        mix.denoise(ids, [seqs[j][t] for j in ids], om)
+        torch.cuda.synchronize()
+        assert torch.equal(oa[0], om[0]), f"frame {t}"
+    alone.close()
+    mix.close()
+
+
+def test_batch_fp16_against_oracle(cuda_dev):
+    sizes = [(48, 27), (80, 45)]
+    frames = 6
+    seqs = _streams(sizes, frames, cuda_dev, f16=True, seed=5)
+    b = Batch(sizes, storage=tg.STORAGE_FP16)
+    P = oracle.full_params()
+    st = [oracle.FullState(h, w, np.float32) for (w, h) in sizes]
+    for t in range(frames):
+        outs = [torch.empty((h, w, 4), dtype=torch.float16, device=cuda_dev) for (w, h) in sizes]
+        b.denoise([0, 1], [seqs[0][t], seqs[1][t]], outs)
+        for j, (w, h) in enumerate(sizes):
+            fr = seqs[j][t]
+            nrm = oracle.oct16_decode(fr["normal"].cpu().numpy())
+            ref, _ = oracle.full_frame(P, st[j], fr["radiance"].float().cpu().numpy(), fr["depth"].cpu().numpy(), nrm,
+                                       fr["motion"].cpu().numpy(), fp16_store=True)
+            g = outs[j].float().cpu().numpy()
+            assert rel_err(g, ref).max() <= 2.0 ** -8
+            assert rel_l2(g, ref) <= 1e-4
+    b.close()
+
+
+def test_autotune_then_reset_state(cuda_dev):
+    sizes = [(64, 36), (160, 90)]
+    seqs = _streams(sizes, 2, cuda_dev)
+    b = Batch(sizes, storage=tg.STORAGE_FP32)
+    outs = [torch.empty((h, w, 4), device=cuda_dev) for (w, h) in sizes]
+    info = b.autotune([0, 1], [seqs[0][0], seqs[1][0]], outs, steps=2)
+    assert info["rows_per_thread"] in (1, 2) and info["ctas_per_sm"] >= 1 and info["tuned_ms"] > 0
+    # state was zeroed: the next step equals a fresh single-stream first frame
+    want = _single(sizes, [s[:1] for s in seqs], tg.STORAGE_FP32, cuda_dev)
+    b.denoise([0, 1], [seqs[0][0], seqs[1][0]], outs)
+    torch.cuda.synchronize()
+    for j in range(2):
+        assert torch.equal(outs[j].cpu(), want[j][0])
+    b.reset_stream(1)
+    b.close()
+
+
+def test_batch_rejects_bad_steps(cuda_dev):
+    b = Batch([(16, 16), (8, 8)], storage=tg.STORAGE_FP32)
+    seqs = _streams([(16, 16), (8, 8)], 1, cuda_dev)
+    outs = [torch.empty((16, 16, 4), device=cuda_dev), torch.empty((8, 8, 4), device=cuda_dev)]
+    with pytest.raises(tg.TgError):
+        b.denoise([0, 0], [seqs[0][0], seqs[0][0]], outs[:1] * 2)
+    with pytest.raises(tg.TgError):
+        b.denoise([5], [seqs[0][0]], outs[:1])
+    with pytest.raises(tg.TgError):  # an 8x8 frame handed to the 16x16 stream: rows too short
+        b.denoise([0], [seqs[1][0]], outs[:1])
+    b.close()

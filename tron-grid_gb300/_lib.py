@@ -58,6 +58,19 @@ class KernelStat(C.Structure):
                 ("total_ms", C.c_double), ("algo_bytes", C.c_double)]
 
 
+class BatchDesc(C.Structure):
+    _fields_ = [("n_streams", C.c_uint32), ("widths", C.POINTER(C.c_uint32)), ("heights", C.POINTER(C.c_uint32)),
+                ("params", Params), ("device", C.c_int32), ("rows_per_thread", C.c_int32),
+                ("ctas_per_sm", C.c_int32), ("use_graph", C.c_int32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("n_streams", C.c_uint32), ("rows_per_thread", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("grid_ctas", C.c_int32), ("graphs", C.c_int32), ("reserved", C.c_int32),
+                ("state_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64), ("steps", C.c_uint64),
+                ("barrier_timeouts", C.c_uint64), ("tuned_ms", C.c_double)]
+
+
 class TgError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{message} (status {status})")
@@ -81,6 +94,15 @@ SIGNATURES = {
     "tg_svgf_state_bytes": (C.c_uint64, [C.POINTER(Params), C.c_uint32, C.c_uint32]),
     "tg_svgf_profile_enable": (C.c_int, [_P, C.c_int]),
     "tg_svgf_profile_read": (C.c_int, [_P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int), C.c_int]),
+    "tg_svgf_batch_create": (C.c_int, [C.POINTER(BatchDesc), C.POINTER(_P)]),
+    "tg_svgf_batch_denoise": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(Inputs),
+                                        C.POINTER(Outputs), _P]),
+    "tg_svgf_batch_autotune": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(Inputs),
+                                         C.POINTER(Outputs), C.c_uint32, _P]),
+    "tg_svgf_batch_reset_stream": (C.c_int, [_P, C.c_uint32, _P]),
+    "tg_svgf_batch_synchronize": (C.c_int, [_P]),
+    "tg_svgf_batch_get_info": (C.c_int, [_P, C.POINTER(BatchInfo)]),
+    "tg_svgf_batch_destroy": (None, [_P]),
     "tg_svgf_denoise_ref_noalloc": (C.c_int, [C.POINTER(Params), C.c_uint32, C.c_uint32, C.POINTER(Image),
                                               C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), _P]),
 }

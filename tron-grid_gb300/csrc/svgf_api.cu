@@ -120,7 +120,7 @@ size_t state_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 
 // Pixels of one a-trous scratch buffer: the largest residue-major layout any
 // level reads or writes (strides 1 .. 2^(levels-1)).
-static size_t col_pixels(const tg_svgf_params& p, uint32_t w, uint32_t h)
+size_t col_pixels_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     size_t n = 0;
     for (int lg = 0; lg < p.levels; ++lg) {
@@ -135,7 +135,7 @@ size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     const size_t n = size_t(w) * h;
     const Layout l = layout_of(p);
-    const size_t col = align_up(col_pixels(p, w, h) * l.c4, 256);
+    const size_t col = align_up(col_pixels_of(p, w, h) * l.c4, 256);
     if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * col;
     return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256);
 }
@@ -239,8 +239,8 @@ void carve(tg_svgf* s)
         s->mom[0] = take(n * l.mom);
         s->mom[1] = take(n * l.mom);
         p = s->scratch;
-        s->colA = take(col_pixels(s->p, s->w, s->h) * l.c4);
-        s->colB = take(col_pixels(s->p, s->w, s->h) * l.c4);
+        s->colA = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
+        s->colB = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
         s->guide[0] = s->guide[1] = s->hist[0] = s->hist[1] = s->tc = nullptr;
         s->grad = nullptr;
     } else {
@@ -251,8 +251,8 @@ void carve(tg_svgf* s)
         }
         p = s->scratch;
         s->tc = take(n * l.c4);
-        s->colA = take(col_pixels(s->p, s->w, s->h) * l.c4);
-        s->colB = take(col_pixels(s->p, s->w, s->h) * l.c4);
+        s->colA = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
+        s->colB = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
         s->grad = static_cast<float2*>(take(n * sizeof(float2)));
     }
 }

@@ -1,0 +1,660 @@
+// Batched SVGF: many streams of uneven resolution in one persistent launch per
+// frame step (include/tg_svgf.h, "batches").
+//
+// Work-list.  A step has 2 + L stages (temporal, variance, L a-trous levels).
+// Stage k of stream j is cut into tiles (32 x 8 pixels for the pixel stages, a
+// residue-class tile for the levels, exactly as in the single-stream kernels);
+// the work table holds, per stage, the exclusive prefix sum of the tile counts
+// over the active streams.  Every CTA of the persistent grid takes items
+// blockIdx.x, blockIdx.x + gridDim.x, ... of the stage, finds its stream by a
+// binary search in the prefix sums, runs the tile, and meets the other CTAs at
+// a grid barrier before the next stage.  The launch is cooperative, so all
+// CTAs are co-resident and the barrier cannot deadlock; its spin is still
+// bounded (about one second), after which it records an error and every CTA
+// returns.
+//
+// Per step the host fills a pinned work table (double buffered) that a CUDA
+// graph copies to the device before the kernel: the graph is captured once per
+// (tile shape, grid) and replayed for any subset of streams.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "svgf_internal.h"
+#include "svgf_kernels.cuh"
+#include "svgf_level.cuh"
+
+namespace tg {
+
+struct BarrierState {
+    unsigned count;
+    unsigned gen;
+    int err;
+    int pad;
+};
+
+struct BatchHeader {
+    int n;        // active streams
+    int levels;
+    int n_stages; // 2 + levels
+    int pad;
+};
+
+struct BatchEntry {
+    FullArgs fa;  // stream-level arguments (col_dst = colA for the variance stage)
+    void* colA;
+    void* colB;
+};
+
+constexpr int kStages = 2 + 10;
+constexpr long long kBarrierSpinCycles = 2000000000LL;  // ~1 s at 2 GHz
+
+__host__ __device__ inline size_t table_prefix_offset() { return sizeof(BatchHeader); }
+__host__ __device__ inline size_t table_entries_offset(int cap)
+{
+    const size_t p = sizeof(BatchHeader) + size_t(kStages) * (cap + 1) * sizeof(int);
+    return (p + 15) / 16 * 16;
+}
+inline size_t table_bytes(int cap) { return table_entries_offset(cap) + size_t(cap) * sizeof(BatchEntry); }
+
+// Grid-wide barrier with a bounded wait.  Returns false when this or any other
+// CTA gave up; the caller then returns.
+__device__ __forceinline__ bool grid_barrier(BarrierState* b, unsigned nblocks)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        ok = 1;
+        volatile unsigned* vgen = &b->gen;
+        volatile int* verr = &b->err;
+        const unsigned g0 = *vgen;
+        __threadfence();
+        if (atomicAdd(&b->count, 1u) == nblocks - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == g0) {
+                if (*verr || clock64() - t0 > kBarrierSpinCycles) {
+                    atomicExch(&b->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int ST, int R>
+__global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __restrict__ table, int cap,
+                                                                   BarrierState* bar)
+{
+    __shared__ LevelSmem<R> sm;
+    const BatchHeader hd = *reinterpret_cast<const BatchHeader*>(table);
+    const int* prefix = reinterpret_cast<const int*>(table + table_prefix_offset());
+    const BatchEntry* ent = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap));
+    for (int stage = 0; stage < hd.n_stages; ++stage) {
+        const int* pf = prefix + stage * (cap + 1);
+        const int items = pf[hd.n];
+        for (int item = blockIdx.x; item < items; item += gridDim.x) {
+            int lo = 0, hi = hd.n;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (pf[mid] <= item)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            const int local = item - pf[lo];
+            const BatchEntry& e = ent[lo];
+            const FullArgs& a = e.fa;
+            if (stage < 2) {
+                const int tx = (a.w + kBlockX - 1) / kBlockX;
+                const int x = (local % tx) * kBlockX + threadIdx.x;
+                const int y = (local / tx) * kBlockY + threadIdx.y;
+                if (x < a.w && y < a.h) {
+                    if (stage == 0)
+                        full_temporal_px<ST>(a, x, y);
+                    else
+                        full_variance_px<ST>(a, x, y);
+                }
+            } else {
+                const int L = stage - 2;
+                LevelArgs lv;
+                lv.col_src = (L & 1) ? e.colB : e.colA;
+                lv.col_dst = (L & 1) ? e.colA : e.colB;
+                lv.level = L;
+                lv.last = L == hd.levels - 1;
+                lv.lin = res_layout(a.w, a.h, L);
+                lv.lout = res_layout(a.w, a.h, L + 1);
+                const LevelGeom g = level_geom(a.w, a.h, 1 << L, R);
+                full_level_tile<ST, R>(a, lv, g, local, sm);
+                __syncthreads();
+            }
+        }
+        if (stage + 1 < hd.n_stages && !grid_barrier(bar, gridDim.x)) return;
+    }
+}
+
+Img to_img(const tg_image& im, uint32_t w);
+
+} // namespace tg
+
+using namespace tg;
+
+struct tg_svgf_batch {
+    int device = 0;
+    tg_svgf_params p{};
+    int n = 0;
+    std::vector<uint32_t> w, h;
+    char* arena = nullptr;
+    size_t state_bytes = 0, scratch_bytes = 0;
+    struct Stream {
+        void* guide[2];
+        void* hist[2];
+        void* mom[2];
+        void* tc;
+        float2* grad;
+        void* colA;
+        void* colB;
+        char* state;
+        size_t state_len;
+        uint64_t frames;
+    };
+    std::vector<Stream> st;
+    int cap = 0;
+    size_t tbytes = 0;
+    char* d_table[2] = {nullptr, nullptr};
+    char* h_table[2] = {nullptr, nullptr};
+    int* h_err = nullptr;  // 2 pinned flags
+    cudaEvent_t table_free[2] = {nullptr, nullptr};
+    bool table_used[2] = {false, false};
+    int tbuf = 0;
+    BarrierState* d_bar = nullptr;
+    int R = 2, ctas = 0, grid = 0;
+    bool use_graph = true, graphs_ok = true;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaStream_t cap_stream = nullptr;
+    uint64_t steps = 0, timeouts = 0;
+    double tuned_ms = 0.0;
+    int sm_count = 0;
+};
+
+namespace {
+
+size_t al256(size_t v) { return (v + 255) / 256 * 256; }
+
+struct DevGuard {
+    int prev = -1;
+    bool sw = false;
+    explicit DevGuard(int d)
+    {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != d) sw = cudaSetDevice(d) == cudaSuccess;
+    }
+    ~DevGuard()
+    {
+        if (sw) cudaSetDevice(prev);
+    }
+};
+
+using KernelFn = void (*)(const char*, int, BarrierState*);
+
+KernelFn kernel_of(bool f16, int R)
+{
+    if (f16) return R == 1 ? k_batch_step<ST_FP16, 1> : k_batch_step<ST_FP16, 2>;
+    return R == 1 ? k_batch_step<ST_FP32, 1> : k_batch_step<ST_FP32, 2>;
+}
+
+int max_ctas_per_sm(bool f16, int R)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel_of(f16, R), kLvTX * kLvRows, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nb;
+}
+
+void drop_graphs(tg_svgf_batch* b)
+{
+    for (auto& e : b->exec)
+        if (e) {
+            cudaGraphExecDestroy(e);
+            e = nullptr;
+        }
+}
+
+int set_config(tg_svgf_batch* b, int R, int ctas)
+{
+    const bool f16 = b->p.storage == TG_SVGF_STORAGE_FP16;
+    const int lim = max_ctas_per_sm(f16, R);
+    if (lim < 1) return fail(TG_ERR_CUDA, "persistent kernel cannot be resident (occupancy query failed)");
+    if (ctas <= 0 || ctas > lim) ctas = lim;
+    b->R = R;
+    b->ctas = ctas;
+    b->grid = ctas * b->sm_count;
+    drop_graphs(b);
+    return TG_OK;
+}
+
+cudaError_t launch_step(tg_svgf_batch* b, int k, cudaStream_t s)
+{
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), s)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(b->d_table[k], b->h_table[k], b->tbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(b->grid);
+    cfg.blockDim = dim3(kLvTX, kLvRows);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const char* tab = b->d_table[k];
+    const int cap = b->cap;
+    BarrierState* bar = b->d_bar;
+    if ((e = cudaLaunchKernelEx(&cfg, kernel_of(b->p.storage == TG_SVGF_STORAGE_FP16, b->R), tab, cap, bar)) !=
+        cudaSuccess)
+        return e;
+    return cudaMemcpyAsync(b->h_err + k, &b->d_bar->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+}
+
+// Captures the step of table buffer k into a graph; on any failure the batch
+// falls back to direct launches.
+void capture(tg_svgf_batch* b, int k)
+{
+    if (!b->use_graph || !b->graphs_ok || b->exec[k]) return;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        b->graphs_ok = false;
+        return;
+    }
+    const cudaError_t le = launch_step(b, k, b->cap_stream);
+    const cudaError_t ee = cudaStreamEndCapture(b->cap_stream, &g);
+    if (le != cudaSuccess || ee != cudaSuccess || !g || cudaGraphInstantiate(&b->exec[k], g, 0) != cudaSuccess) {
+        cudaGetLastError();
+        b->exec[k] = nullptr;
+        b->graphs_ok = false;
+    }
+    if (g) cudaGraphDestroy(g);
+}
+
+int check_stream_inputs(const tg_svgf_batch* b, uint32_t id, const tg_svgf_inputs& in, const tg_svgf_outputs& out)
+{
+    static const int rad[] = {TG_FMT_RGBA32F, TG_FMT_RGBA16F};
+    static const int dep[] = {TG_FMT_R32F};
+    static const int nrm[] = {TG_FMT_RGB32F, TG_FMT_RGBA32F, TG_FMT_OCT16};
+    static const int mot[] = {TG_FMT_RG32F, TG_FMT_RG16F};
+    const uint32_t W = b->w[id], H = b->h[id];
+    int st;
+    if ((st = check_image("radiance", in.radiance, W, H, rad, 2))) return st;
+    if ((st = check_image("depth", in.depth, W, H, dep, 1))) return st;
+    if ((st = check_image("normal", in.normal, W, H, nrm, 3))) return st;
+    if ((st = check_image("motion", in.motion, W, H, mot, 2))) return st;
+    if ((st = check_image("denoised", out.denoised, W, H, rad, 2))) return st;
+    return TG_OK;
+}
+
+// Fills host table k for this step and advances the streams' frame counters.
+void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const tg_svgf_inputs* in,
+                const tg_svgf_outputs* out)
+{
+    char* t = b->h_table[k];
+    std::memset(t, 0, b->tbytes);
+    BatchHeader* hd = reinterpret_cast<BatchHeader*>(t);
+    hd->n = int(n);
+    hd->levels = b->p.levels;
+    hd->n_stages = 2 + b->p.levels;
+    int* prefix = reinterpret_cast<int*>(t + table_prefix_offset());
+    BatchEntry* ent = reinterpret_cast<BatchEntry*>(t + table_entries_offset(b->cap));
+    for (int stage = 0; stage < hd->n_stages; ++stage) {
+        int* pf = prefix + stage * (b->cap + 1);
+        int acc = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+            pf[j] = acc;
+            const int W = int(b->w[ids[j]]), H = int(b->h[ids[j]]);
+            if (stage < 2)
+                acc += ((W + kBlockX - 1) / kBlockX) * ((H + kBlockY - 1) / kBlockY);
+            else
+                acc += int(level_blocks(level_geom(W, H, 1 << (stage - 2), b->R)));
+        }
+        pf[n] = acc;
+    }
+    for (uint32_t j = 0; j < n; ++j) {
+        tg_svgf_batch::Stream& s = b->st[ids[j]];
+        const int cur = int(s.frames & 1u), prev = cur ^ 1;
+        const uint32_t W = b->w[ids[j]];
+        FullArgs& a = ent[j].fa;
+        a.w = int(W);
+        a.h = int(b->h[ids[j]]);
+        a.radiance = to_img(in[j].radiance, W);
+        a.depth = to_img(in[j].depth, W);
+        a.normal = to_img(in[j].normal, W);
+        a.motion = to_img(in[j].motion, W);
+        a.out = to_img(out[j].denoised, W);
+        a.guide_prev = s.guide[prev];
+        a.hist_prev = s.hist[prev];
+        a.mom_prev = s.mom[prev];
+        a.guide_cur = s.guide[cur];
+        a.hist_cur = s.hist[cur];
+        a.mom_cur = s.mom[cur];
+        a.tc = s.tc;
+        a.grad = s.grad;
+        a.col_dst = s.colA;
+        a.alpha = b->p.alpha;
+        a.alpha_m = b->p.moments_alpha;
+        a.sigma_l = b->p.sigma_l;
+        a.sigma_n = b->p.sigma_n;
+        a.sigma_z = b->p.sigma_z;
+        a.sq_n = sigma_n_squarings(b->p.sigma_n);
+        a.max_history = b->p.max_history;
+        a.fallback_frames = b->p.fallback_frames;
+        ent[j].colA = s.colA;
+        ent[j].colB = s.colB;
+        s.frames++;
+    }
+}
+
+// Waits until host table k may be rewritten and collects its step's barrier flag.
+int reclaim(tg_svgf_batch* b, int k)
+{
+    if (!b->table_used[k]) return TG_OK;
+    if (cudaEventSynchronize(b->table_free[k]) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "batch step failed: %s", cudaGetErrorString(cudaGetLastError()));
+    b->table_used[k] = false;
+    if (b->h_err[k]) {
+        b->h_err[k] = 0;
+        b->timeouts++;
+        return fail(TG_ERR_TIMEOUT, "a batch step's grid barrier gave up; that step's outputs are invalid");
+    }
+    return TG_OK;
+}
+
+int run_step(tg_svgf_batch* b, uint32_t n, const uint32_t* ids, const tg_svgf_inputs* in, const tg_svgf_outputs* out,
+             cudaStream_t stream)
+{
+    const int k = b->tbuf;
+    int st = reclaim(b, k);
+    if (st == TG_ERR_CUDA) return st;
+    fill_table(b, k, n, ids, in, out);
+    capture(b, k);
+    cudaError_t e;
+    if (b->exec[k])
+        e = cudaGraphLaunch(b->exec[k], stream);
+    else
+        e = launch_step(b, k, stream);
+    if (e != cudaSuccess) return fail(TG_ERR_CUDA, "batch step launch failed: %s", cudaGetErrorString(e));
+    if (cudaEventRecord(b->table_free[k], stream) != cudaSuccess) return fail(TG_ERR_CUDA, "event record failed");
+    b->table_used[k] = true;
+    b->tbuf ^= 1;
+    b->steps++;
+    return st;
+}
+
+void free_batch(tg_svgf_batch* b)
+{
+    drop_graphs(b);
+    for (int k = 0; k < 2; ++k) {
+        if (b->d_table[k]) cudaFree(b->d_table[k]);
+        if (b->h_table[k]) cudaFreeHost(b->h_table[k]);
+        if (b->table_free[k]) cudaEventDestroy(b->table_free[k]);
+    }
+    if (b->h_err) cudaFreeHost(b->h_err);
+    if (b->d_bar) cudaFree(b->d_bar);
+    if (b->arena) cudaFree(b->arena);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+}
+
+} // namespace
+
+extern "C" {
+
+int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
+{
+    if (!d || !out) return fail(TG_ERR_INVALID, "null descriptor or output");
+    *out = nullptr;
+    if (d->n_streams < 1 || d->n_streams > TG_SVGF_BATCH_MAX_STREAMS || !d->widths || !d->heights)
+        return fail(TG_ERR_INVALID, "n_streams must be 1..%d with widths and heights", TG_SVGF_BATCH_MAX_STREAMS);
+    if (d->params.mode != TG_SVGF_MODE_FULL) return fail(TG_ERR_INVALID, "batches run the FULL mode");
+    int st = validate_params(d->params);
+    if (st) return st;
+    if (d->rows_per_thread < 0 || d->rows_per_thread > 2) return fail(TG_ERR_INVALID, "rows_per_thread must be 0..2");
+    for (uint32_t j = 0; j < d->n_streams; ++j)
+        if (d->widths[j] == 0 || d->heights[j] == 0 || d->widths[j] > 32768 || d->heights[j] > 32768)
+            return fail(TG_ERR_INVALID, "stream %u: size %ux%u outside 1..32768", j, d->widths[j], d->heights[j]);
+    int dev = d->device;
+    if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) return fail(TG_ERR_CUDA, "no current CUDA device");
+    DevGuard g(dev);
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) {
+        cudaGetLastError();
+        return fail(TG_ERR_UNSUPPORTED, "device %d cannot launch cooperative kernels", dev);
+    }
+    tg_svgf_batch* b = new (std::nothrow) tg_svgf_batch();
+    if (!b) return fail(TG_ERR_OOM, "host allocation failed");
+    b->device = dev;
+    b->p = d->params;
+    b->n = int(d->n_streams);
+    b->w.assign(d->widths, d->widths + d->n_streams);
+    b->h.assign(d->heights, d->heights + d->n_streams);
+    b->use_graph = d->use_graph != 0;
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    const bool f16 = b->p.storage == TG_SVGF_STORAGE_FP16;
+    const size_t gb = f16 ? 8 : 16, c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
+    // arena: per stream [state | scratch]
+    std::vector<size_t> off(b->n + 1, 0);
+    for (int j = 0; j < b->n; ++j) {
+        const size_t np = size_t(b->w[j]) * b->h[j];
+        const size_t sb = state_bytes_of(b->p, b->w[j], b->h[j]);
+        const size_t cb = al256(np * c4) + al256(np * sizeof(float2)) + 2 * al256(col_pixels_of(b->p, b->w[j], b->h[j]) * c4);
+        b->state_bytes += sb;
+        b->scratch_bytes += cb;
+        off[j + 1] = off[j] + sb + cb;
+    }
+    auto cleanup = [&](int status) {
+        free_batch(b);
+        delete b;
+        return status;
+    };
+    if (cudaMalloc(&b->arena, off[b->n]) != cudaSuccess) {
+        cudaGetLastError();
+        b->arena = nullptr;
+        return cleanup(fail(TG_ERR_OOM, "cudaMalloc of %zu batch bytes failed", off[b->n]));
+    }
+    b->st.resize(b->n);
+    for (int j = 0; j < b->n; ++j) {
+        const size_t np = size_t(b->w[j]) * b->h[j];
+        char* p = b->arena + off[j];
+        tg_svgf_batch::Stream& s = b->st[j];
+        s.state = p;
+        s.state_len = state_bytes_of(b->p, b->w[j], b->h[j]);
+        for (int k = 0; k < 2; ++k) {
+            s.guide[k] = p;
+            p += al256(np * gb);
+            s.hist[k] = p;
+            p += al256(np * c4);
+            s.mom[k] = p;
+            p += al256(np * mm);
+        }
+        s.tc = p;
+        p += al256(np * c4);
+        s.grad = reinterpret_cast<float2*>(p);
+        p += al256(np * sizeof(float2));
+        const size_t colb = al256(col_pixels_of(b->p, b->w[j], b->h[j]) * c4);
+        s.colA = p;
+        p += colb;
+        s.colB = p;
+        s.frames = 0;
+    }
+    if (cudaMemset(b->arena, 0, off[b->n]) != cudaSuccess) return cleanup(fail(TG_ERR_CUDA, "arena clear failed"));
+    b->cap = b->n;
+    b->tbytes = table_bytes(b->cap);
+    for (int k = 0; k < 2; ++k) {
+        if (cudaMalloc(&b->d_table[k], b->tbytes) != cudaSuccess ||
+            cudaHostAlloc(reinterpret_cast<void**>(&b->h_table[k]), b->tbytes, cudaHostAllocDefault) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->table_free[k], cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return cleanup(fail(TG_ERR_OOM, "work table allocation failed"));
+        }
+    }
+    if (cudaHostAlloc(reinterpret_cast<void**>(&b->h_err), 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess ||
+        cudaMalloc(&b->d_bar, sizeof(BarrierState)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(fail(TG_ERR_OOM, "barrier allocation failed"));
+    }
+    b->h_err[0] = b->h_err[1] = 0;
+    if (cudaMemset(b->d_bar, 0, sizeof(BarrierState)) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
+        return cleanup(fail(TG_ERR_CUDA, "batch initialisation failed"));
+    st = set_config(b, d->rows_per_thread ? d->rows_per_thread : 2, d->ctas_per_sm);
+    if (st) return cleanup(st);
+    *out = b;
+    return TG_OK;
+}
+
+static int check_step(tg_svgf_batch* b, uint32_t n, const uint32_t* ids, const tg_svgf_inputs* in,
+                      const tg_svgf_outputs* out)
+{
+    if (!b) return fail(TG_ERR_INVALID, "null batch");
+    if (n == 0) return TG_OK;
+    if (!ids || !in || !out) return fail(TG_ERR_INVALID, "null stream ids, inputs or outputs");
+    if (n > uint32_t(b->n)) return fail(TG_ERR_INVALID, "more streams than the batch holds");
+    std::vector<char> seen(b->n, 0);
+    for (uint32_t j = 0; j < n; ++j) {
+        if (ids[j] >= uint32_t(b->n)) return fail(TG_ERR_INVALID, "stream id %u out of range", ids[j]);
+        if (seen[ids[j]]) return fail(TG_ERR_INVALID, "stream %u listed twice in one step", ids[j]);
+        seen[ids[j]] = 1;
+        int st = check_stream_inputs(b, ids[j], in[j], out[j]);
+        if (st) return st;
+    }
+    return TG_OK;
+}
+
+int tg_svgf_batch_denoise(tg_svgf_batch* b, uint32_t n, const uint32_t* ids, const tg_svgf_inputs* in,
+                          const tg_svgf_outputs* out, void* stream)
+{
+    int st = check_step(b, n, ids, in, out);
+    if (st || n == 0) return st;
+    DevGuard g(b->device);
+    return run_step(b, n, ids, in, out, static_cast<cudaStream_t>(stream));
+}
+
+int tg_svgf_batch_autotune(tg_svgf_batch* b, uint32_t n, const uint32_t* ids, const tg_svgf_inputs* in,
+                           const tg_svgf_outputs* out, uint32_t steps, void* stream_v)
+{
+    int st = check_step(b, n, ids, in, out);
+    if (st) return st;
+    if (n == 0 || steps == 0) return fail(TG_ERR_INVALID, "autotune needs streams and steps");
+    DevGuard g(b->device);
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+    const bool f16 = b->p.storage == TG_SVGF_STORAGE_FP16;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "event creation failed");
+    double best = 1e30;
+    int bestR = b->R, bestC = b->ctas;
+    for (int R = 1; R <= 2; ++R) {
+        const int lim = max_ctas_per_sm(f16, R);
+        for (int c = 1; c <= lim; ++c) {
+            if ((st = set_config(b, R, c))) break;
+            if ((st = run_step(b, n, ids, in, out, stream)) != TG_OK) break;  // warm-up, also captures
+            if ((st = run_step(b, n, ids, in, out, stream)) != TG_OK) break;
+            cudaEventRecord(e0, stream);
+            for (uint32_t k = 0; k < steps && st == TG_OK; ++k) st = run_step(b, n, ids, in, out, stream);
+            cudaEventRecord(e1, stream);
+            if (st) break;
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                st = fail(TG_ERR_CUDA, "autotune step failed");
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms / steps < best) {
+                best = ms / steps;
+                bestR = R;
+                bestC = c;
+            }
+        }
+        if (st) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int k = 0; k < 2; ++k) {
+        const int r = reclaim(b, k);
+        if (!st) st = r;
+    }
+    if (st) return st;
+    if ((st = set_config(b, bestR, bestC))) return st;
+    b->tuned_ms = best;
+    // tuning advanced every stream: zero all state
+    for (auto& s : b->st) {
+        if (cudaMemsetAsync(s.state, 0, s.state_len, stream) != cudaSuccess)
+            return fail(TG_ERR_CUDA, "state clear failed");
+        s.frames = 0;
+    }
+    return TG_OK;
+}
+
+int tg_svgf_batch_reset_stream(tg_svgf_batch* b, uint32_t id, void* stream)
+{
+    if (!b) return fail(TG_ERR_INVALID, "null batch");
+    if (id >= uint32_t(b->n)) return fail(TG_ERR_INVALID, "stream id %u out of range", id);
+    DevGuard g(b->device);
+    tg_svgf_batch::Stream& s = b->st[id];
+    if (cudaMemsetAsync(s.state, 0, s.state_len, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "state clear failed");
+    s.frames = 0;
+    return TG_OK;
+}
+
+int tg_svgf_batch_synchronize(tg_svgf_batch* b)
+{
+    if (!b) return fail(TG_ERR_INVALID, "null batch");
+    DevGuard g(b->device);
+    int st = TG_OK;
+    for (int k = 0; k < 2; ++k) {
+        const int r = reclaim(b, k);
+        if (!st) st = r;
+    }
+    return st;
+}
+
+int tg_svgf_batch_get_info(const tg_svgf_batch* b, tg_svgf_batch_info* info)
+{
+    if (!b || !info) return fail(TG_ERR_INVALID, "null batch or info");
+    std::memset(info, 0, sizeof *info);
+    info->n_streams = uint32_t(b->n);
+    info->rows_per_thread = b->R;
+    info->ctas_per_sm = b->ctas;
+    info->grid_ctas = b->grid;
+    info->graphs = (b->use_graph && b->graphs_ok) ? 1 : 0;
+    info->state_bytes = b->state_bytes;
+    info->scratch_bytes = b->scratch_bytes;
+    info->steps = b->steps;
+    info->barrier_timeouts = b->timeouts;
+    info->tuned_ms = b->tuned_ms;
+    return TG_OK;
+}
+
+void tg_svgf_batch_destroy(tg_svgf_batch* b)
+{
+    if (!b) return;
+    DevGuard g(b->device);
+    cudaDeviceSynchronize();
+    free_batch(b);
+    delete b;
+}
+
+} // extern "C"

@@ -25,5 +25,7 @@ int validate_params(const tg_svgf_params& p);
 int sigma_n_squarings(float sigma_n);
 size_t state_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
+// Pixels of one a-trous scratch image in the largest residue-major layout used.
+size_t col_pixels_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 
 } // namespace tg

@@ -29,7 +29,7 @@ __device__ __forceinline__ size_t res_idx(const ResLayout& L, int x, int y)
     return (size_t(((y & m) << L.lg) + (x & m)) * L.ph + (y >> L.lg)) * L.pw + (x >> L.lg);
 }
 
-inline ResLayout res_layout(int w, int h, int lg)
+__host__ __device__ inline ResLayout res_layout(int w, int h, int lg)
 {
     ResLayout L;
     L.lg = lg;
@@ -106,15 +106,12 @@ struct FullArgs {
 
 // K1: guide write, reprojection (bilinear 2x2 with depth/normal test), history
 // length, colour EMA and mean-centred moment EMA.
-template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_temporal(FullArgs a)
+template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArgs& a, int x, int y)
 {
     typedef Stor<ST> S;
     typedef typename S::guide_t G;
     typedef typename S::c4_t C4;
     typedef typename S::mom_t M;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    if (x >= a.w || y >= a.h) return;
     const size_t i = size_t(y) * a.w + x;
 
     uint32_t enc = 0;
@@ -214,15 +211,12 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_tem
 // K2: variance per pixel: the temporal moment variance, or for histories
 // shorter than `fallback_frames` a 7x7 depth/normal-weighted spatial estimate
 // from the neighbours' moments.  Writes col = (colour, variance).
-template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_variance(FullArgs a)
+template <int ST> __device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y)
 {
     typedef Stor<ST> S;
     typedef typename S::guide_t G;
     typedef typename S::c4_t C4;
     typedef typename S::mom_t M;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    if (x >= a.w || y >= a.h) return;
     const size_t i = size_t(y) * a.w + x;
     const C4* tc = static_cast<const C4*>(a.tc);
     const M* mc = static_cast<const M*>(a.mom_cur);
@@ -264,6 +258,20 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_var
         }
     }
     S::st4_sat_w(static_cast<C4*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var));
+}
+
+template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_temporal(FullArgs a)
+{
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y * kBlockY + threadIdx.y;
+    if (x < a.w && y < a.h) full_temporal_px<ST>(a, x, y);
+}
+
+template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_variance(FullArgs a)
+{
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y * kBlockY + threadIdx.y;
+    if (x < a.w && y < a.h) full_variance_px<ST>(a, x, y);
 }
 
 } // namespace tg

@@ -55,12 +55,19 @@ template <int R> struct LevelTile {
     static constexpr int N = SW * SH;
 };
 
-// Maps this block to (residue a, b) and its tile origin in sub-lattice units.
-__device__ __forceinline__ void level_block(const LevelGeom& g, int TX, int TY, int& ra, int& rb, int& i0, int& j0)
+template <int R> struct LevelSmem {
+    float4 A[LevelTile<R>::N];
+    float4 N[LevelTile<R>::N];
+    float V[LevelTile<R>::N];
+};
+
+// Maps tile `bid` to (residue a, b) and its tile origin in sub-lattice units.
+__device__ __forceinline__ void level_block(const LevelGeom& g, int bid, int TX, int TY, int& ra, int& rb, int& i0,
+                                            int& j0)
 {
     const int ss = g.s * g.s;
-    const int res = blockIdx.x % ss;
-    const int tile = blockIdx.x / ss;
+    const int res = bid % ss;
+    const int tile = bid / ss;
     ra = res % g.s;
     rb = res / g.s;
     i0 = (tile % g.tiles_x) * TX;
@@ -69,22 +76,45 @@ __device__ __forceinline__ void level_block(const LevelGeom& g, int TX, int TY, 
 
 // ------------------------------------------------------------------ FULL ----
 
-template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_full_level_tiled(FullArgs a, LevelGeom g)
+// Per-level arguments of an a-trous level (the rest comes from FullArgs).
+struct LevelArgs {
+    const void* col_src;
+    void* col_dst;
+    int level, last;
+    ResLayout lin, lout;
+};
+
+__host__ __device__ inline LevelArgs level_args_of(const FullArgs& a)
+{
+    LevelArgs l;
+    l.col_src = a.col_src;
+    l.col_dst = a.col_dst;
+    l.level = a.level;
+    l.last = a.last;
+    l.lin = a.lin;
+    l.lout = a.lout;
+    return l;
+}
+
+// One tile of one level.  The caller synchronises the CTA before reusing `sm`.
+template <int ST, int R>
+__device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
+                                                LevelSmem<R>& sm)
 {
     typedef Stor<ST> S;
     typedef typename S::guide_t G;
     typedef typename S::c4_t C4;
     typedef LevelTile<R> T;
-    __shared__ float4 sA[T::N];
-    __shared__ float4 sN[T::N];
-    __shared__ float sV[T::N];
+    float4* sA = sm.A;
+    float4* sN = sm.N;
+    float* sV = sm.V;
 
     int ra, rb, i0, j0;
-    level_block(g, T::TX, T::TY, ra, rb, i0, j0);
-    const int s = g.s, lg = a.lin.lg, m = s - 1;
-    const int pw = a.lin.pw;
-    const int P = a.lin.pw * a.lin.ph;  // elements per residue plane (< 2^31)
-    const C4* src = static_cast<const C4*>(a.col_src);
+    level_block(g, bid, T::TX, T::TY, ra, rb, i0, j0);
+    const int s = g.s, lg = lv.lin.lg, m = s - 1;
+    const int pw = lv.lin.pw;
+    const int P = lv.lin.pw * lv.lin.ph;  // elements per residue plane (< 2^31)
+    const C4* src = static_cast<const C4*>(lv.col_src);
     const G* gc = static_cast<const G*>(a.guide_cur);
     const int ci = threadIdx.x;         // tile column of this thread's outputs
     const int cj0 = threadIdx.y * R;    // first tile row of this thread's outputs
@@ -220,15 +250,21 @@ template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_
             const int c = (cj0 + k + 2) * T::SW + ci + 2;
             o = make_float4(sA[c].x, sA[c].y, sA[c].z, sV[c]);
         }
-        if (a.level == 0) {
+        if (lv.level == 0) {
             const float len = S::ld4_w(static_cast<const C4*>(a.tc), i);
             S::st4(static_cast<C4*>(a.hist_cur), i, make_float4(o.x, o.y, o.z, len));
         }
-        if (a.last)
+        if (lv.last)
             st_rgba(a.out, cx, y, make_float4(S::qin(o.x), S::qin(o.y), S::qin(o.z), 1.0f));
         else
-            S::st4_sat_w(static_cast<C4*>(a.col_dst), res_idx(a.lout, cx, y), o);
+            S::st4_sat_w(static_cast<C4*>(lv.col_dst), res_idx(lv.lout, cx, y), o);
     }
+}
+
+template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_full_level_tiled(FullArgs a, LevelGeom g)
+{
+    __shared__ LevelSmem<R> sm;
+    full_level_tile<ST, R>(a, level_args_of(a), g, blockIdx.x, sm);
 }
 
 // ------------------------------------------------------------- REF-EXACT ----
@@ -243,7 +279,7 @@ template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref
     __shared__ float4 sA[T::N];
 
     int ra, rb, i0, j0;
-    level_block(g, T::TX, T::TY, ra, rb, i0, j0);
+    level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
     const int s = g.s;
     const C4* src = static_cast<const C4*>(a.src);
     const int tid = threadIdx.y * kLvTX + threadIdx.x;
@@ -308,7 +344,7 @@ template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref
     }
 }
 
-inline LevelGeom level_geom(int w, int h, int s, int R)
+__host__ __device__ inline LevelGeom level_geom(int w, int h, int s, int R)
 {
     LevelGeom g;
     g.s = s;
@@ -319,6 +355,9 @@ inline LevelGeom level_geom(int w, int h, int s, int R)
     return g;
 }
 
-inline unsigned level_blocks(const LevelGeom& g) { return unsigned(g.s * g.s) * g.tiles_x * g.tiles_y; }
+__host__ __device__ inline unsigned level_blocks(const LevelGeom& g)
+{
+    return unsigned(g.s * g.s) * g.tiles_x * g.tiles_y;
+}
 
 } // namespace tg
