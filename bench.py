@@ -53,6 +53,9 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-profile", action="store_true", help="no per-kernel events in the timed region")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP16 / REF_EXACT / batched / accuracy lines")
+    ap.add_argument("--batch-streams", type=int, default=64)
+    ap.add_argument("--batch-frames", type=int, default=30)
     return ap.parse_args(argv)
 
 
@@ -316,9 +319,194 @@ def run_tg(args, rank, world, local):
         res["e2e"] = None
     del frames
     torch.cuda.empty_cache()
+    if not args.no_extras and args.mode == "full" and args.storage == "fp32":
+        res["fp16_4k"] = run_single(args, dev, "full", "fp16", steps=min(args.steps, 120))
+        res["ref_exact_4k"] = run_single(args, dev, "ref", "fp16", steps=min(args.steps, 120))
+        res["batched"] = run_batched(args, dev)
+        if rank == 0:
+            res["accuracy"] = run_accuracy(dev)
+        torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu:
         res["cpu_baseline"] = run_cpu_baseline(args, spec, seconds=args.cpu_seconds)
     return res
+
+
+def run_single(args, dev, mode_s, storage_s, steps):
+    """Device-timed frames/s of one stream in another mode/storage on the same 4K sequence."""
+    import torch
+
+    import tron_grid_gb300 as tg
+
+    spec, _ = workload(args)
+    W, H = spec.width, spec.height
+    frames = gen_frames(spec, min(args.pool, 30), dev, storage_s, mode_s)
+    mode = tg.MODE_FULL if mode_s == "full" else tg.MODE_REF_EXACT
+    storage = tg.STORAGE_FP32 if storage_s == "fp32" else tg.STORAGE_FP16
+    dt = torch.float32 if storage_s == "fp32" else torch.float16
+    out = torch.empty((H, W, 4), dtype=dt, device=dev)
+    den = tg.Denoiser(W, H, mode=mode, storage=storage, device=dev.index)
+    stream = torch.cuda.current_stream()
+
+    def step(i):
+        fr = frames[i % len(frames)]
+        den.denoise(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=out)
+
+    for i in range(5):
+        step(i)
+    den.profile(True)
+    den.profile_read(reset=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        step(5 + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    prof = den.profile_read(reset=True)
+    den.close()
+    bpp = algo_bytes_per_px(mode_s, storage_s)
+    peak, _ = load_peaks()
+    return {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "mpx_per_s": W * H / ms / 1e3,
+            "algo_bytes_per_px": bpp, "chain_hbm_frac": bpp * W * H / (ms / 1e3) / 1e9 / peak,
+            "kernels": {k: {"launches": v["launches"], "avg_ms": v["total_ms"] / max(v["launches"], 1),
+                            "gbs": v["algo_bytes"] / max(v["total_ms"], 1e-12) / 1e6} for k, v in prof.items()},
+            "workload": f"{'FULL' if mode_s == 'full' else 'REF_EXACT'} {W}x{H} {storage_s.upper()} storage"}
+
+
+def run_batched(args, dev):
+    """BASELINE config 3: N streams of seeded resolutions, FP16, one persistent launch per step (autotuned,
+    graph-replayed), against the plain per-stream FP32 path on the same frames."""
+    import numpy as np
+    import torch
+
+    import tron_grid_gb300 as tg
+    from tron_grid_gb300 import scene
+    from tron_grid_gb300.batch import Batch
+
+    res_set = [(160, 90), (320, 180), (640, 360), (1280, 720)]
+    specs = scene.stream_specs(args.batch_streams, res_set, seed=3, frames=args.batch_frames)
+    sizes = [(s.width, s.height) for s in specs]
+    F = args.batch_frames
+    f32 = []
+    f16 = []
+    for sp in specs:
+        sc = scene.PlaneScene(sp, device=dev)
+        a32, a16 = [], []
+        for t in range(F):
+            fr = sc.frame(t)
+            d = {k: fr[k] for k in KEYS}
+            a32.append(d)
+            a16.append({"radiance": d["radiance"].half(), "depth": d["depth"],
+                        "normal": scene.oct16_encode(d["normal"]), "motion": d["motion"]})
+        f32.append(a32)
+        f16.append(a16)
+    torch.cuda.synchronize()
+    px = sum(w * h for w, h in sizes)
+    ids = list(range(len(sizes)))
+    warm = 3
+    stream = torch.cuda.current_stream()
+
+    # batched FP16
+    b = Batch(sizes, storage=tg.STORAGE_FP16)
+    outs16 = [torch.empty((h, w, 4), dtype=torch.float16, device=dev) for (w, h) in sizes]
+    tune = b.autotune(ids, [f16[j][0] for j in ids], outs16, steps=3)
+    for t in range(warm):
+        b.denoise(ids, [f16[j][t] for j in ids], outs16)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(F - warm + 1)]
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for t in range(warm, F):
+        b.denoise(ids, [f16[j][t] for j in ids], outs16)
+        evs[t - warm + 1].record(stream)
+    b.synchronize()
+    torch.cuda.synchronize()
+    bt = sorted(evs[i].elapsed_time(evs[i + 1]) for i in range(F - warm))
+    binfo = b.info()
+    b.close()
+
+    # plain per-stream FP32: one handle per stream, one call per stream per step
+    dens = [tg.Denoiser(w, h, storage=tg.STORAGE_FP32, device=dev.index) for (w, h) in sizes]
+    outs32 = [torch.empty((h, w, 4), device=dev) for (w, h) in sizes]
+    for t in range(warm):
+        for j in ids:
+            fr = f32[j][t]
+            dens[j].denoise(fr["radiance"], fr["depth"], fr["normal"], fr["motion"], out=outs32[j])
+    pevs = [torch.cuda.Event(enable_timing=True) for _ in range(F - warm + 1)]
+    torch.cuda.synchronize()
+    pevs[0].record(stream)
+    for t in range(warm, F):
+        for j in ids:
+            fr = f32[j][t]
+            dens[j].denoise(fr["radiance"], fr["depth"], fr["normal"], fr["motion"], out=outs32[j])
+        pevs[t - warm + 1].record(stream)
+    torch.cuda.synchronize()
+    pt = sorted(pevs[i].elapsed_time(pevs[i + 1]) for i in range(F - warm))
+    for d in dens:
+        d.close()
+    # error of the batched FP16 result against the plain FP32 result (last frame, luminance)
+    Y = torch.tensor([0.2126, 0.7152, 0.0722], device=dev)
+    errs = []
+    for j in ids:
+        la = (outs16[j][..., :3].float() * Y).sum(-1)
+        lb = (outs32[j][..., :3] * Y).sum(-1)
+        errs.append(float(torch.sqrt(((la - lb) ** 2).sum() / (lb ** 2).sum().clamp_min(1e-30))))
+    q = lambda v, f: v[min(len(v) - 1, int(f * len(v)))]
+    b_mpx = px * len(bt) / (sum(bt) / 1e3) / 1e6
+    p_mpx = px * len(pt) / (sum(pt) / 1e3) / 1e6
+    return {"workload": f"{len(sizes)} streams from {res_set} (seeded), FULL, {F} frames, batched FP16 vs plain FP32",
+            "total_px_per_step": px, "streams_by_size": {f"{w}x{h}": sizes.count((w, h)) for (w, h) in res_set},
+            "batched": {"mpx_per_s": b_mpx, "p50_ms": q(bt, 0.5), "p99_ms": q(bt, 0.99),
+                        "launches_per_step": 1, "rows_per_thread": binfo["rows_per_thread"],
+                        "ctas_per_sm": binfo["ctas_per_sm"], "graphs": binfo["graphs"],
+                        "tuned_ms": tune["tuned_ms"], "barrier_timeouts": binfo["barrier_timeouts"]},
+            "plain": {"mpx_per_s": p_mpx, "p50_ms": q(pt, 0.5), "p99_ms": q(pt, 0.99),
+                      "launches_per_step": 7 * len(sizes)},
+            "speedup_mpx": b_mpx / p_mpx, "rel_l2_vs_plain_max": max(errs)}
+
+
+def run_accuracy(dev, frames=33):
+    """Per-frame error of the FP32 and FP16 GPU paths against the float64 oracle (640x360, config-1 motion)."""
+    import numpy as np
+    import torch
+
+    import oracle
+    import tron_grid_gb300 as tg
+    from tron_grid_gb300 import scene
+
+    W, H = 640, 360
+    sc = scene.PlaneScene(scene.config1(W, H, seed=0))
+    d32 = tg.Denoiser(W, H, storage=tg.STORAGE_FP32, device=dev.index)
+    d16 = tg.Denoiser(W, H, storage=tg.STORAGE_FP16, device=dev.index)
+    st = oracle.FullState(H, W, np.float64)
+    P = oracle.full_params()
+    Y = np.array([0.2126, 0.7152, 0.0722])
+    rows = {"fp32": [], "fp16": []}
+    for t in range(frames):
+        fr = sc.frame(t)
+        ref, _ = oracle.full_frame(P, st, *(fr[k].numpy() for k in KEYS))
+        lr = ref[..., :3] @ Y
+        o32 = d32.denoise(*(fr[k].to(dev) for k in KEYS))
+        enc = oracle.oct16_encode(fr["normal"].numpy())
+        o16 = torch.empty((H, W, 4), dtype=torch.float16, device=dev)
+        d16.denoise(fr["radiance"].half().to(dev), fr["depth"].to(dev), torch.from_numpy(enc).to(dev),
+                    fr["motion"].to(dev), out=o16)
+        for name, o in (("fp32", o32), ("fp16", o16)):
+            lg = o.float().cpu().numpy()[..., :3] @ Y
+            d = lg - lr
+            mse = float(np.mean(d * d))
+            rows[name].append({"max_abs": float(np.abs(d).max()),
+                               "max_rel": float((np.abs(d) / np.maximum(np.abs(lr), 1e-3)).max()),
+                               "rel_l2": float(np.sqrt((d * d).sum() / (lr * lr).sum())),
+                               "psnr_db": float(10 * np.log10(lr.max() ** 2 / mse)) if mse > 0 else None})
+    d32.close()
+    d16.close()
+    out = {"workload": f"FULL {W}x{H}, {frames} frames (camera yaw + translation, plane at frame 30), vs float64 oracle"}
+    for name, r in rows.items():
+        ps = [x["psnr_db"] for x in r if x["psnr_db"] is not None]
+        out[name] = {"max_abs": max(x["max_abs"] for x in r), "max_rel": max(x["max_rel"] for x in r),
+                     "rel_l2_max": max(x["rel_l2"] for x in r), "psnr_db_min": min(ps) if ps else None}
+    return out
 
 
 def run_e2e(args, frames, dev, mode, storage, world):

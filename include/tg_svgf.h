@@ -229,6 +229,9 @@ typedef struct tg_svgf_batch_desc {
     int32_t rows_per_thread;   /* a-trous outputs per thread (tile 32 x 8r): 1 or 2; 0 = 2 until autotuned */
     int32_t ctas_per_sm;       /* persistent CTAs per SM: 1..3; 0 = the occupancy limit */
     int32_t use_graph;         /* nonzero: replay each step from a captured CUDA graph */
+    uint32_t barrier_timeout_us; /* bound of each grid-barrier wait; 0 = about one second */
+    int32_t debug_barrier_extra; /* test hook: the barrier also waits for this many CTAs that do not
+                                    exist, so every step's wait runs out (TG_ERR_TIMEOUT); 0 otherwise */
 } tg_svgf_batch_desc;
 
 typedef struct tg_svgf_batch_info {
@@ -269,6 +272,70 @@ TG_API int tg_svgf_batch_synchronize(tg_svgf_batch* b);
 TG_API int tg_svgf_batch_get_info(const tg_svgf_batch* b, tg_svgf_batch_info* info);
 
 TG_API void tg_svgf_batch_destroy(tg_svgf_batch* b);
+
+/* ---------------------------------------------------------------- serving --
+ * A request loop over many sessions (camera streams that come and go): frames
+ * are submitted from any host thread with host buffers and complete
+ * asynchronously.  With batching on, a scheduler thread admits every queued
+ * frame whose session has a free slot (one frame per session per batch, in
+ * arrival order), copies the batch's inputs in while the previous batch runs,
+ * and denoises the batch in one persistent launch (continuous batching); with
+ * batching off every request is launched on its own (the plain per-request
+ * path).  Each session's history stays resident on the device inside an HBM
+ * budget: a session that does not fit evicts the least recently used idle
+ * session (one with no queued or running frame); an evicted session's next
+ * frame restarts as a full disocclusion.  FULL mode only. */
+typedef struct tg_svgf_server tg_svgf_server;
+
+typedef struct tg_svgf_server_desc {
+    tg_svgf_params params;     /* mode must be TG_SVGF_MODE_FULL */
+    uint64_t hbm_budget_bytes; /* device bytes for resident sessions (state, scratch, staging) */
+    uint32_t max_sessions;     /* sessions known at once (resident or not) */
+    uint32_t max_batch;        /* frames per launch, 1 .. TG_SVGF_BATCH_MAX_STREAMS */
+    int32_t device;            /* -1 = current */
+    int32_t batching;          /* 1: continuous batching; 0: plain per-request launches */
+    int32_t use_graph;         /* batching: replay launches from CUDA graphs */
+    int32_t reserved;
+} tg_svgf_server_desc;
+
+typedef struct tg_svgf_request_info {
+    int32_t status;      /* TG_OK, TG_ERR_BUDGET (session larger than the budget), TG_ERR_STATE (session ended) ... */
+    uint32_t batch_size; /* frames in the launch that carried this request */
+    double latency_ms;   /* submit -> result in host memory */
+    double queue_ms;     /* submit -> launch */
+} tg_svgf_request_info;
+
+typedef struct tg_svgf_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t admissions, evictions, launches;
+    uint64_t resident_bytes, peak_resident_bytes;
+    uint32_t resident_sessions, max_batch_seen;
+    double p50_ms, p99_ms, mean_ms; /* latency of completed requests since the last reset */
+    double mpx_per_s;               /* pixels completed / (last completion - first submit) */
+    double wall_s;
+} tg_svgf_server_stats;
+
+TG_API int tg_svgf_server_create(const tg_svgf_server_desc* desc, tg_svgf_server** out);
+
+/* Queues one frame of `session` (width x height; host inputs/outputs, kept
+ * alive and unmodified until the ticket completes; pinned for overlap). */
+TG_API int tg_svgf_server_submit(tg_svgf_server* s, uint64_t session, uint32_t width, uint32_t height,
+                                 const tg_svgf_inputs* host_inputs, const tg_svgf_outputs* host_outputs,
+                                 uint64_t* ticket);
+
+/* Waits for a ticket (timeout_us < 0: no limit); TG_ERR_TIMEOUT if it did not
+ * complete in time, else TG_OK with the request's own status in info.  A
+ * completed ticket is forgotten once waited for. */
+TG_API int tg_svgf_server_wait(tg_svgf_server* s, uint64_t ticket, int64_t timeout_us, tg_svgf_request_info* info);
+
+/* Ends a session: its queued frames fail with TG_ERR_STATE and its device
+ * memory is released once no frame of it is running. */
+TG_API int tg_svgf_server_end_session(tg_svgf_server* s, uint64_t session);
+
+TG_API int tg_svgf_server_get_stats(tg_svgf_server* s, tg_svgf_server_stats* stats, int reset);
+
+/* Stops the scheduler after the queued work and frees everything. */
+TG_API void tg_svgf_server_destroy(tg_svgf_server* s);
 
 /* Reference-exact frame for callers that cannot allocate device memory.
  * This entry point has no counterpart in the reference.  It exists for callers

@@ -61,7 +61,8 @@ class KernelStat(C.Structure):
 class BatchDesc(C.Structure):
     _fields_ = [("n_streams", C.c_uint32), ("widths", C.POINTER(C.c_uint32)), ("heights", C.POINTER(C.c_uint32)),
                 ("params", Params), ("device", C.c_int32), ("rows_per_thread", C.c_int32),
-                ("ctas_per_sm", C.c_int32), ("use_graph", C.c_int32)]
+                ("ctas_per_sm", C.c_int32), ("use_graph", C.c_int32), ("barrier_timeout_us", C.c_uint32),
+                ("debug_barrier_extra", C.c_int32)]
 
 
 class BatchInfo(C.Structure):
@@ -69,6 +70,26 @@ class BatchInfo(C.Structure):
                 ("grid_ctas", C.c_int32), ("graphs", C.c_int32), ("reserved", C.c_int32),
                 ("state_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64), ("steps", C.c_uint64),
                 ("barrier_timeouts", C.c_uint64), ("tuned_ms", C.c_double)]
+
+
+class ServerDesc(C.Structure):
+    _fields_ = [("params", Params), ("hbm_budget_bytes", C.c_uint64), ("max_sessions", C.c_uint32),
+                ("max_batch", C.c_uint32), ("device", C.c_int32), ("batching", C.c_int32),
+                ("use_graph", C.c_int32), ("reserved", C.c_int32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_size", C.c_uint32), ("latency_ms", C.c_double),
+                ("queue_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("admissions", C.c_uint64), ("evictions", C.c_uint64), ("launches", C.c_uint64),
+                ("resident_bytes", C.c_uint64), ("peak_resident_bytes", C.c_uint64),
+                ("resident_sessions", C.c_uint32), ("max_batch_seen", C.c_uint32),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("mpx_per_s", C.c_double), ("wall_s", C.c_double)]
 
 
 class TgError(RuntimeError):
@@ -103,6 +124,13 @@ SIGNATURES = {
     "tg_svgf_batch_synchronize": (C.c_int, [_P]),
     "tg_svgf_batch_get_info": (C.c_int, [_P, C.POINTER(BatchInfo)]),
     "tg_svgf_batch_destroy": (None, [_P]),
+    "tg_svgf_server_create": (C.c_int, [C.POINTER(ServerDesc), C.POINTER(_P)]),
+    "tg_svgf_server_submit": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(Inputs),
+                                        C.POINTER(Outputs), C.POINTER(C.c_uint64)]),
+    "tg_svgf_server_wait": (C.c_int, [_P, C.c_uint64, C.c_int64, C.POINTER(RequestInfo)]),
+    "tg_svgf_server_end_session": (C.c_int, [_P, C.c_uint64]),
+    "tg_svgf_server_get_stats": (C.c_int, [_P, C.POINTER(ServerStats), C.c_int]),
+    "tg_svgf_server_destroy": (None, [_P]),
     "tg_svgf_denoise_ref_noalloc": (C.c_int, [C.POINTER(Params), C.c_uint32, C.c_uint32, C.POINTER(Image),
                                               C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), _P]),
 }

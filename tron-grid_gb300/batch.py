@@ -13,7 +13,8 @@ class Batch:
     """N camera streams of their own resolutions, FULL mode, denoised step by step."""
 
     def __init__(self, sizes, storage: int = L.STORAGE_FP16, device: int | None = None, rows_per_thread: int = 0,
-                 ctas_per_sm: int = 0, use_graph: bool = True, **params):
+                 ctas_per_sm: int = 0, use_graph: bool = True, barrier_timeout_us: int = 0,
+                 debug_barrier_extra: int = 0, **params):
         self.lib = L.load()
         self.sizes = [(int(w), int(h)) for (w, h) in sizes]
         n = len(self.sizes)
@@ -22,7 +23,8 @@ class Batch:
         if device is None:
             device = torch.cuda.current_device()
         self.params = L.default_params(L.MODE_FULL, storage, **params)
-        d = L.BatchDesc(n, ws, hs, self.params, device, rows_per_thread, ctas_per_sm, int(use_graph))
+        d = L.BatchDesc(n, ws, hs, self.params, device, rows_per_thread, ctas_per_sm, int(use_graph),
+                        barrier_timeout_us, debug_barrier_extra)
         h = C.c_void_p()
         L.check(self.lib.tg_svgf_batch_create(C.byref(d), C.byref(h)))
         self.handle = h

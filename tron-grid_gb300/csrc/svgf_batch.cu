@@ -1,17 +1,6 @@
 // Batched SVGF: many streams of uneven resolution in one persistent launch per
-// frame step (include/tg_svgf.h, "batches").
-//
-// Work-list.  A step has 2 + L stages (temporal, variance, L a-trous levels).
-// Stage k of stream j is cut into tiles (32 x 8 pixels for the pixel stages, a
-// residue-class tile for the levels, exactly as in the single-stream kernels);
-// the work table holds, per stage, the exclusive prefix sum of the tile counts
-// over the active streams.  Every CTA of the persistent grid takes items
-// blockIdx.x, blockIdx.x + gridDim.x, ... of the stage, finds its stream by a
-// binary search in the prefix sums, runs the tile, and meets the other CTAs at
-// a grid barrier before the next stage.  The launch is cooperative, so all
-// CTAs are co-resident and the barrier cannot deadlock; its spin is still
-// bounded (about one second), after which it records an error and every CTA
-// returns.
+// frame step (include/tg_svgf.h, "batches"); the kernel and its work table are
+// in svgf_batch_kernel.cuh.
 //
 // Per step the host fills a pinned work table (double buffered) that a CUDA
 // graph copies to the device before the kernel: the graph is captured once per
@@ -23,126 +12,10 @@
 #include <new>
 #include <vector>
 
+#include "svgf_batch_kernel.cuh"
 #include "svgf_internal.h"
-#include "svgf_kernels.cuh"
-#include "svgf_level.cuh"
 
 namespace tg {
-
-struct BarrierState {
-    unsigned count;
-    unsigned gen;
-    int err;
-    int pad;
-};
-
-struct BatchHeader {
-    int n;        // active streams
-    int levels;
-    int n_stages; // 2 + levels
-    int pad;
-};
-
-struct BatchEntry {
-    FullArgs fa;  // stream-level arguments (col_dst = colA for the variance stage)
-    void* colA;
-    void* colB;
-};
-
-constexpr int kStages = 2 + 10;
-constexpr long long kBarrierSpinCycles = 2000000000LL;  // ~1 s at 2 GHz
-
-__host__ __device__ inline size_t table_prefix_offset() { return sizeof(BatchHeader); }
-__host__ __device__ inline size_t table_entries_offset(int cap)
-{
-    const size_t p = sizeof(BatchHeader) + size_t(kStages) * (cap + 1) * sizeof(int);
-    return (p + 15) / 16 * 16;
-}
-inline size_t table_bytes(int cap) { return table_entries_offset(cap) + size_t(cap) * sizeof(BatchEntry); }
-
-// Grid-wide barrier with a bounded wait.  Returns false when this or any other
-// CTA gave up; the caller then returns.
-__device__ __forceinline__ bool grid_barrier(BarrierState* b, unsigned nblocks)
-{
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        ok = 1;
-        volatile unsigned* vgen = &b->gen;
-        volatile int* verr = &b->err;
-        const unsigned g0 = *vgen;
-        __threadfence();
-        if (atomicAdd(&b->count, 1u) == nblocks - 1) {
-            atomicExch(&b->count, 0u);
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*vgen == g0) {
-                if (*verr || clock64() - t0 > kBarrierSpinCycles) {
-                    atomicExch(&b->err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
-template <int ST, int R>
-__global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __restrict__ table, int cap,
-                                                                   BarrierState* bar)
-{
-    __shared__ LevelSmem<R> sm;
-    const BatchHeader hd = *reinterpret_cast<const BatchHeader*>(table);
-    const int* prefix = reinterpret_cast<const int*>(table + table_prefix_offset());
-    const BatchEntry* ent = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap));
-    for (int stage = 0; stage < hd.n_stages; ++stage) {
-        const int* pf = prefix + stage * (cap + 1);
-        const int items = pf[hd.n];
-        for (int item = blockIdx.x; item < items; item += gridDim.x) {
-            int lo = 0, hi = hd.n;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (pf[mid] <= item)
-                    lo = mid;
-                else
-                    hi = mid;
-            }
-            const int local = item - pf[lo];
-            const BatchEntry& e = ent[lo];
-            const FullArgs& a = e.fa;
-            if (stage < 2) {
-                const int tx = (a.w + kBlockX - 1) / kBlockX;
-                const int x = (local % tx) * kBlockX + threadIdx.x;
-                const int y = (local / tx) * kBlockY + threadIdx.y;
-                if (x < a.w && y < a.h) {
-                    if (stage == 0)
-                        full_temporal_px<ST>(a, x, y);
-                    else
-                        full_variance_px<ST>(a, x, y);
-                }
-            } else {
-                const int L = stage - 2;
-                LevelArgs lv;
-                lv.col_src = (L & 1) ? e.colB : e.colA;
-                lv.col_dst = (L & 1) ? e.colA : e.colB;
-                lv.level = L;
-                lv.last = L == hd.levels - 1;
-                lv.lin = res_layout(a.w, a.h, L);
-                lv.lout = res_layout(a.w, a.h, L + 1);
-                const LevelGeom g = level_geom(a.w, a.h, 1 << L, R);
-                full_level_tile<ST, R>(a, lv, g, local, sm);
-                __syncthreads();
-            }
-        }
-        if (stage + 1 < hd.n_stages && !grid_barrier(bar, gridDim.x)) return;
-    }
-}
 
 Img to_img(const tg_image& im, uint32_t w);
 
@@ -186,6 +59,8 @@ struct tg_svgf_batch {
     uint64_t steps = 0, timeouts = 0;
     double tuned_ms = 0.0;
     int sm_count = 0;
+    long long spin_cycles = kBarrierSpinCycles;
+    int barrier_extra = 0;
 };
 
 namespace {
@@ -205,7 +80,7 @@ struct DevGuard {
     }
 };
 
-using KernelFn = void (*)(const char*, int, BarrierState*);
+using KernelFn = void (*)(const char*, int, BarrierState*, unsigned, long long);
 
 KernelFn kernel_of(bool f16, int R)
 {
@@ -264,8 +139,10 @@ cudaError_t launch_step(tg_svgf_batch* b, int k, cudaStream_t s)
     const char* tab = b->d_table[k];
     const int cap = b->cap;
     BarrierState* bar = b->d_bar;
-    if ((e = cudaLaunchKernelEx(&cfg, kernel_of(b->p.storage == TG_SVGF_STORAGE_FP16, b->R), tab, cap, bar)) !=
-        cudaSuccess)
+    const unsigned expect = unsigned(b->grid + b->barrier_extra);
+    const long long spin = b->spin_cycles;
+    if ((e = cudaLaunchKernelEx(&cfg, kernel_of(b->p.storage == TG_SVGF_STORAGE_FP16, b->R), tab, cap, bar, expect,
+                                spin)) != cudaSuccess)
         return e;
     return cudaMemcpyAsync(b->h_err + k, &b->d_bar->err, sizeof(int), cudaMemcpyDeviceToHost, s);
 }
@@ -451,6 +328,12 @@ int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
     b->h.assign(d->heights, d->heights + d->n_streams);
     b->use_graph = d->use_graph != 0;
     cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (d->barrier_timeout_us > 0) {
+        int khz = 0;
+        cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev);
+        b->spin_cycles = (long long)d->barrier_timeout_us * (khz > 0 ? khz : 2000000) / 1000;
+    }
+    b->barrier_extra = d->debug_barrier_extra > 0 ? d->debug_barrier_extra : 0;
     const bool f16 = b->p.storage == TG_SVGF_STORAGE_FP16;
     const size_t gb = f16 ? 8 : 16, c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
     // arena: per stream [state | scratch]

@@ -1,0 +1,138 @@
+// The persistent multi-stream step kernel, its work table and its bounded
+// grid barrier: shared by the batched form (svgf_batch.cu) and the serving
+// loop (svgf_serve.cu).
+//
+// Work-list.  A step has 2 + L stages (temporal, variance, L a-trous levels).
+// Stage k of stream j is cut into tiles (32 x 8 pixels for the pixel stages, a
+// residue-class tile for the levels, exactly as in the single-stream kernels);
+// the work table holds, per stage, the exclusive prefix sum of the tile counts
+// over the active streams.  Every CTA of the persistent grid takes items
+// blockIdx.x, blockIdx.x + gridDim.x, ... of the stage, finds its stream by a
+// binary search in the prefix sums, runs the tile, and meets the other CTAs at
+// a grid barrier before the next stage.  The launch is cooperative, so all
+// CTAs are co-resident and the barrier cannot deadlock; its spin is still
+// bounded, after which it records an error and every CTA returns.
+#pragma once
+
+#include "svgf_kernels.cuh"
+#include "svgf_level.cuh"
+
+namespace tg {
+
+struct BarrierState {
+    unsigned count;
+    unsigned gen;
+    int err;
+    int pad;
+};
+
+struct BatchHeader {
+    int n;        // active streams
+    int levels;
+    int n_stages; // 2 + levels
+    int pad;
+};
+
+struct BatchEntry {
+    FullArgs fa;  // stream-level arguments (col_dst = colA for the variance stage)
+    void* colA;
+    void* colB;
+};
+
+constexpr int kStages = 2 + 10;
+constexpr long long kBarrierSpinCycles = 2000000000LL;  // default limit, ~1 s at 2 GHz
+
+__host__ __device__ inline size_t table_prefix_offset() { return sizeof(BatchHeader); }
+__host__ __device__ inline size_t table_entries_offset(int cap)
+{
+    const size_t p = sizeof(BatchHeader) + size_t(kStages) * (cap + 1) * sizeof(int);
+    return (p + 15) / 16 * 16;
+}
+inline size_t table_bytes(int cap) { return table_entries_offset(cap) + size_t(cap) * sizeof(BatchEntry); }
+
+// Grid-wide barrier with a bounded wait.  Returns false when this or any other
+// CTA gave up; the caller then returns.
+__device__ __forceinline__ bool grid_barrier(BarrierState* b, unsigned nblocks, long long spin_cycles)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        ok = 1;
+        volatile unsigned* vgen = &b->gen;
+        volatile int* verr = &b->err;
+        const unsigned g0 = *vgen;
+        __threadfence();
+        if (atomicAdd(&b->count, 1u) == nblocks - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == g0) {
+                if (*verr || clock64() - t0 > spin_cycles) {
+                    atomicExch(&b->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int ST, int R>
+__global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __restrict__ table, int cap,
+                                                                   BarrierState* bar, unsigned expect_blocks,
+                                                                   long long spin_cycles)
+{
+    __shared__ LevelSmem<R> sm;
+    const BatchHeader hd = *reinterpret_cast<const BatchHeader*>(table);
+    const int* prefix = reinterpret_cast<const int*>(table + table_prefix_offset());
+    const BatchEntry* ent = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap));
+    for (int stage = 0; stage < hd.n_stages; ++stage) {
+        const int* pf = prefix + stage * (cap + 1);
+        const int items = pf[hd.n];
+        for (int item = blockIdx.x; item < items; item += gridDim.x) {
+            int lo = 0, hi = hd.n;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (pf[mid] <= item)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            const int local = item - pf[lo];
+            const BatchEntry& e = ent[lo];
+            const FullArgs& a = e.fa;
+            if (stage < 2) {
+                const int tx = (a.w + kBlockX - 1) / kBlockX;
+                const int x = (local % tx) * kBlockX + threadIdx.x;
+                const int y = (local / tx) * kBlockY + threadIdx.y;
+                if (x < a.w && y < a.h) {
+                    if (stage == 0)
+                        full_temporal_px<ST>(a, x, y);
+                    else
+                        full_variance_px<ST>(a, x, y);
+                }
+            } else {
+                const int L = stage - 2;
+                LevelArgs lv;
+                lv.col_src = (L & 1) ? e.colB : e.colA;
+                lv.col_dst = (L & 1) ? e.colA : e.colB;
+                lv.level = L;
+                lv.last = L == hd.levels - 1;
+                lv.lin = res_layout(a.w, a.h, L);
+                lv.lout = res_layout(a.w, a.h, L + 1);
+                const LevelGeom g = level_geom(a.w, a.h, 1 << L, R);
+                full_level_tile<ST, R>(a, lv, g, local, sm);
+                __syncthreads();
+            }
+        }
+        if (stage + 1 < hd.n_stages && !grid_barrier(bar, expect_blocks, spin_cycles)) return;
+    }
+}
+
+} // namespace tg

@@ -142,6 +142,24 @@ __device__ __forceinline__ float3 oct16_decode(uint32_t u)
     return make_float3(__fmul_rn(px, inv), __fmul_rn(py, inv), __fmul_rn(vz, inv));
 }
 
+// Octahedral decode for edge-stopping weights only (never for a discrete
+// decision): reciprocal-multiply and rsqrt instead of IEEE divisions.
+__device__ __forceinline__ float3 oct16_decode_fast(uint32_t u)
+{
+    const float kInv = 1.0f / 32767.0f;
+    float px = fmaxf(-1.0f, float(int(int16_t(u & 0xffffu))) * kInv);
+    float py = fmaxf(-1.0f, float(int(int16_t(u >> 16))) * kInv);
+    const float vz = 1.0f - fabsf(px) - fabsf(py);
+    if (vz < 0.0f) {
+        const float ox = (1.0f - fabsf(py)) * sgn_nz(px);
+        const float oy = (1.0f - fabsf(px)) * sgn_nz(py);
+        px = ox;
+        py = oy;
+    }
+    const float inv = rsqrtf(fmaf(px, px, fmaf(py, py, vz * vz)));
+    return make_float3(px * inv, py * inv, vz * inv);
+}
+
 // ---------------------------------------------------------- caller images ----
 
 __device__ __forceinline__ const char* row_ptr(const Img& im, int y) { return im.ptr + int64_t(y) * im.pitch; }
@@ -213,6 +231,7 @@ template <> struct Stor<ST_FP32> {
     typedef float4 c4_t;
     typedef float2 mom_t;
     __device__ static float4 ld_guide(const guide_t* p, size_t i) { return __ldg(p + i); }
+    __device__ static float4 ld_guide_w(const guide_t* p, size_t i) { return __ldg(p + i); }
     __device__ static float ld_guide_z(const guide_t* p, size_t i) { return __ldg(reinterpret_cast<const float*>(p + i) + 3); }
     __device__ static guide_t mk_guide(float3 n, uint32_t, float z) { return make_float4(n.x, n.y, n.z, z); }
     __device__ static float4 ld4(const c4_t* p, size_t i) { return __ldg(p + i); }
@@ -232,6 +251,13 @@ template <> struct Stor<ST_FP16> {
     {
         uint2 u = __ldg(p + i);
         float3 n = oct16_decode(u.x);
+        return make_float4(n.x, n.y, n.z, __uint_as_float(u.y));
+    }
+    // guide for edge-stopping weights (fast decode)
+    __device__ static float4 ld_guide_w(const guide_t* p, size_t i)
+    {
+        uint2 u = __ldg(p + i);
+        float3 n = oct16_decode_fast(u.x);
         return make_float4(n.x, n.y, n.z, __uint_as_float(u.y));
     }
     __device__ static float ld_guide_z(const guide_t* p, size_t i)

@@ -163,7 +163,7 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
             const float4 c = S::ld4(src, plane + j * pw + i);
             va = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
             vv = c.w;
-            vn = S::ld_guide(gc, y * a.w + x);
+            vn = S::ld_guide_w(gc, y * a.w + x);
         }
         sA[k] = va;
         sN[k] = vn;
@@ -207,31 +207,38 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
     }
 
     // ---- taps: rows r = 0 .. R+3 of this thread's strip, 5 columns each.
+    // A warp (one strip row of 32 columns) whose outputs all lie outside the
+    // sub-lattice skips the taps.
+    bool any_valid = false;
+#pragma unroll
+    for (int k = 0; k < R; ++k) any_valid |= valid[k];
     const float sn = a.sigma_n;
+    if (__any_sync(0xffffffffu, any_valid)) {
 #pragma unroll
-    for (int r = 0; r < R + 4; ++r) {
+        for (int r = 0; r < R + 4; ++r) {
 #pragma unroll
-        for (int dx = -2; dx <= 2; ++dx) {
-            const int q = (cj0 + r) * T::SW + ci + 2 + dx;
-            const float4 A = sA[q], N = sN[q];
-            const float V = sV[q];
+            for (int dx = -2; dx <= 2; ++dx) {
+                const int q = (cj0 + r) * T::SW + ci + 2 + dx;
+                const float4 A = sA[q], N = sN[q];
+                const float V = sV[q];
 #pragma unroll
-            for (int k = 0; k < R; ++k) {
-                const int dy = r - 2 - k;
-                if (dy < -2 || dy > 2) continue;
-                const int ddx = (dy > 0 || (dy == 0 && dx >= 0)) ? dx : -dx;
-                const int ddy = dy >= 0 ? dy : -dy;
-                const int qi = ddy == 0 ? ddx : 3 + (ddy - 1) * 5 + (ddx + 2);
-                const float d = fmaf(nz[k], N.z, fmaf(ny[k], N.y, nx[k] * N.x));
-                float t = fmaf(-fabsf(zp[k] - N.w), kz[k][qi], log2_b3(dx + 2) + log2_b3(dy + 2));
-                t = fmaf(-fabsf(lp[k] - A.w), kl[k], t);
-                t = fmaf(sn, lg2_approx(fmaxf(d, 0.f)), t);
-                const float w = ex2_approx(t);
-                ar[k] = fmaf(w, A.x, ar[k]);
-                ag[k] = fmaf(w, A.y, ag[k]);
-                ab[k] = fmaf(w, A.z, ab[k]);
-                aw[k] += w;
-                av[k] = fmaf(w * w, V, av[k]);
+                for (int k = 0; k < R; ++k) {
+                    const int dy = r - 2 - k;
+                    if (dy < -2 || dy > 2) continue;
+                    const int ddx = (dy > 0 || (dy == 0 && dx >= 0)) ? dx : -dx;
+                    const int ddy = dy >= 0 ? dy : -dy;
+                    const int qi = ddy == 0 ? ddx : 3 + (ddy - 1) * 5 + (ddx + 2);
+                    const float d = fmaf(nz[k], N.z, fmaf(ny[k], N.y, nx[k] * N.x));
+                    float t = fmaf(-fabsf(zp[k] - N.w), kz[k][qi], log2_b3(dx + 2) + log2_b3(dy + 2));
+                    t = fmaf(-fabsf(lp[k] - A.w), kl[k], t);
+                    t = fmaf(sn, lg2_approx(fmaxf(d, 0.f)), t);
+                    const float w = ex2_approx(t);
+                    ar[k] = fmaf(w, A.x, ar[k]);
+                    ag[k] = fmaf(w, A.y, ag[k]);
+                    ab[k] = fmaf(w, A.z, ab[k]);
+                    aw[k] += w;
+                    av[k] = fmaf(w * w, V, av[k]);
+                }
             }
         }
     }
