@@ -56,6 +56,9 @@ def parse_args(argv=None):
     ap.add_argument("--no-extras", action="store_true", help="skip the FP16 / REF_EXACT / batched / accuracy lines")
     ap.add_argument("--batch-streams", type=int, default=64)
     ap.add_argument("--batch-frames", type=int, default=30)
+    ap.add_argument("--serve-sessions", type=int, default=256)
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-rate", type=float, default=4000.0)
     return ap.parse_args(argv)
 
 
@@ -323,6 +326,7 @@ def run_tg(args, rank, world, local):
         res["fp16_4k"] = run_single(args, dev, "full", "fp16", steps=min(args.steps, 120))
         res["ref_exact_4k"] = run_single(args, dev, "ref", "fp16", steps=min(args.steps, 120))
         res["batched"] = run_batched(args, dev)
+        res["serving"] = run_serving(args, dev)
         if rank == 0:
             res["accuracy"] = run_accuracy(dev)
         torch.cuda.empty_cache()
@@ -463,6 +467,99 @@ def run_batched(args, dev):
             "plain": {"mpx_per_s": p_mpx, "p50_ms": q(pt, 0.5), "p99_ms": q(pt, 0.99),
                       "launches_per_step": 7 * len(sizes)},
             "speedup_mpx": b_mpx / p_mpx, "rel_l2_vs_plain_max": max(errs)}
+
+
+def run_serving(args, dev):
+    """BASELINE config 4: sessions of seeded resolutions submit frames as a Poisson process (aggregate rate),
+    each session alternating exponential(2 s) idle and active periods; continuous batching (FP16 storage)
+    against plain per-request launches (FP32 storage) on the same arrivals; 24 GB budget."""
+    import numpy as np
+    import torch
+
+    import tron_grid_gb300 as tg
+    from tron_grid_gb300 import scene
+    from tron_grid_gb300.serve import Server
+
+    res_set = [(160, 90), (320, 180), (640, 360), (1280, 720), (1920, 1080)]
+    weights = [0.3, 0.3, 0.2, 0.15, 0.05]
+    n = args.serve_sessions
+    specs = scene.stream_specs(n, res_set, weights=weights, seed=7, frames=2)
+    host = []
+    for sp in specs:
+        sc = scene.PlaneScene(sp, device=dev)
+        fr2 = []
+        for t in range(2):
+            fr = sc.frame(t)
+            d = {"radiance": fr["radiance"].half(), "depth": fr["depth"], "normal": scene.oct16_encode(fr["normal"]),
+                 "motion": fr["motion"]}
+            fr2.append({k: v.cpu().pin_memory() for k, v in d.items()})
+        host.append(fr2)
+    ring = 4
+    outs = [[torch.empty((sp.height, sp.width, 4), dtype=torch.float16, pin_memory=True) for _ in range(ring)]
+            for sp in specs]
+    # arrivals: aggregate Poisson process over the sessions that are active at that moment
+    rng = np.random.default_rng(11)
+    T = args.serve_seconds
+    switch = []
+    for j in range(n):
+        t, on, ev = 0.0, bool(rng.random() < 0.5), []
+        while t < T:
+            t += rng.exponential(2.0)
+            ev.append(t)
+        switch.append((on, np.array(ev)))
+
+    def active(j, t):
+        on, ev = switch[j]
+        return on ^ bool(np.searchsorted(ev, t) % 2)
+
+    arrivals = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / args.serve_rate)
+        if t >= T:
+            break
+        act = [j for j in range(n) if active(j, t)] or list(range(n))
+        arrivals.append((t, int(rng.choice(act))))
+
+    def run(server, paced):
+        counts = [0] * n
+        pending = {}
+        lat = []
+        t0 = time.perf_counter()
+        for (ta, j) in arrivals:
+            if paced:
+                while time.perf_counter() - t0 < ta:
+                    pass
+            slot = counts[j] % ring
+            key = (j, slot)
+            if key in pending:  # the ring slot's previous frame must be done before its buffer is reused
+                lat.append(server.wait(pending.pop(key)))
+            pending[key] = server.submit(j, host[j][counts[j] % 2], outs[j][slot])
+            counts[j] += 1
+        for tk in list(pending.values()):
+            lat.append(server.wait(tk))
+        st = server.stats()
+        return st
+
+    out = {"workload": f"{n} sessions from {res_set} (weights {weights}), Poisson {args.serve_rate:.0f} frames/s for "
+                       f"{T:.0f} s, exponential(2 s) idle/active periods, 24 GB budget, FP16 inputs",
+           "requests": len(arrivals),
+           "offered_mpx_per_s": sum(specs[j].width * specs[j].height for _, j in arrivals) / T / 1e6}
+    for name, kw in (("batched", dict(batching=True, storage=tg.STORAGE_FP16, max_batch=min(n, 256))),
+                     ("plain", dict(batching=False, storage=tg.STORAGE_FP32, max_batch=1))):
+        sv = Server(24 << 30, max_sessions=n + 8, device=dev.index, **kw)
+        res = {}
+        for mode, paced in (("offered", True), ("saturated", False)):
+            st = run(sv, paced)
+            res[mode] = {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                         "mpx_per_s": st["mpx_per_s"], "completed": st["completed"], "failed": st["failed"],
+                         "launches": st["launches"], "max_batch": st["max_batch_seen"],
+                         "evictions": st["evictions"], "peak_resident_gb": st["peak_resident_bytes"] / 2 ** 30}
+            sv.stats(reset=True)
+        sv.close()
+        out[name] = res
+    out["saturated_speedup_mpx"] = out["batched"]["saturated"]["mpx_per_s"] / max(out["plain"]["saturated"]["mpx_per_s"], 1e-9)
+    return out
 
 
 def run_accuracy(dev, frames=33):

@@ -439,8 +439,8 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +
                            fmt_bytes(in->normal.format) + fmt_bytes(in->motion.format);
         const double ob = fmt_bytes(out->denoised.format);
-        // temporal: inputs + previous guide/history/moments, writes guide, tc, moments
-        launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm)), [&] {
+        // temporal: inputs + previous guide/history/moments, writes guide, tc, moments, depth gradient
+        launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm) + 8), [&] {
             if (f16)
                 k_full_temporal<ST_FP16><<<grd, blk, 0, stream>>>(a);
             else
@@ -463,8 +463,8 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             a.last = lv == s->p.levels - 1;
             a.lin = res_layout(a.w, a.h, lv);
             a.lout = res_layout(a.w, a.h, lv + 1);
-            // level: col + guide in, col (or output) out; level 0 also tc in, history out
-            const double lb = c4 + gb + (a.last ? ob : c4) + (lv == 0 ? 2 * c4 : 0);
+            // level: col + guide + depth gradient in, col (or output) out; level 0 also tc in, history out
+            const double lb = c4 + gb + 8 + (a.last ? ob : c4) + (lv == 0 ? 2 * c4 : 0);
             const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
             const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
             launch(s, stream, F_FULL_LEVEL, npx * lb, [&] {
