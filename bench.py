@@ -461,7 +461,9 @@ def run_batched(args, dev):
     return {"workload": f"{len(sizes)} streams from {res_set} (seeded), FULL, {F} frames, batched FP16 vs plain FP32",
             "total_px_per_step": px, "streams_by_size": {f"{w}x{h}": sizes.count((w, h)) for (w, h) in res_set},
             "batched": {"mpx_per_s": b_mpx, "p50_ms": q(bt, 0.5), "p99_ms": q(bt, 0.99),
-                        "launches_per_step": 1, "rows_per_thread": binfo["rows_per_thread"],
+                        "strategy": "persistent" if binfo["strategy"] == 1 else "stages",
+                        "launches_per_step": 1 if binfo["strategy"] == 1 else 7,
+                        "rows_per_thread": binfo["rows_per_thread"],
                         "ctas_per_sm": binfo["ctas_per_sm"], "graphs": binfo["graphs"],
                         "tuned_ms": tune["tuned_ms"], "barrier_timeouts": binfo["barrier_timeouts"]},
             "plain": {"mpx_per_s": p_mpx, "p50_ms": q(pt, 0.5), "p99_ms": q(pt, 0.99),

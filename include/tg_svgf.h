@@ -218,6 +218,13 @@ TG_API int tg_svgf_profile_read(tg_svgf* h, tg_svgf_kernel_stat* stats, int capa
  * device; a stream's result is identical alone and in any mix of streams. */
 #define TG_SVGF_BATCH_MAX_STREAMS 1024
 
+/* How a step runs: one kernel launch per stage over the work-list of all the
+ * step's streams (7 launches per step with 5 levels, whatever the number of
+ * streams), or one persistent cooperative launch with a grid barrier between
+ * stages.  tg_svgf_batch_autotune measures both. */
+#define TG_SVGF_BATCH_STAGES 0
+#define TG_SVGF_BATCH_PERSISTENT 1
+
 typedef struct tg_svgf_batch tg_svgf_batch;
 
 typedef struct tg_svgf_batch_desc {
@@ -229,6 +236,7 @@ typedef struct tg_svgf_batch_desc {
     int32_t rows_per_thread;   /* a-trous outputs per thread (tile 32 x 8r): 1 or 2; 0 = 2 until autotuned */
     int32_t ctas_per_sm;       /* persistent CTAs per SM: 1..3; 0 = the occupancy limit */
     int32_t use_graph;         /* nonzero: replay each step from a captured CUDA graph */
+    int32_t strategy;          /* TG_SVGF_BATCH_STAGES (default) or TG_SVGF_BATCH_PERSISTENT */
     uint32_t barrier_timeout_us; /* bound of each grid-barrier wait; 0 = about one second */
     int32_t debug_barrier_extra; /* test hook: the barrier also waits for this many CTAs that do not
                                     exist, so every step's wait runs out (TG_ERR_TIMEOUT); 0 otherwise */
@@ -240,7 +248,7 @@ typedef struct tg_svgf_batch_info {
     int32_t ctas_per_sm;
     int32_t grid_ctas;         /* persistent grid size */
     int32_t graphs;            /* 1 when steps replay CUDA graphs */
-    int32_t reserved;
+    int32_t strategy;          /* TG_SVGF_BATCH_STAGES or TG_SVGF_BATCH_PERSISTENT */
     uint64_t state_bytes;      /* device state of all streams */
     uint64_t scratch_bytes;    /* device scratch of all streams */
     uint64_t steps;            /* frame steps run */
@@ -257,8 +265,9 @@ TG_API int tg_svgf_batch_create(const tg_svgf_batch_desc* desc, tg_svgf_batch** 
 TG_API int tg_svgf_batch_denoise(tg_svgf_batch* b, uint32_t n, const uint32_t* stream_ids,
                                  const tg_svgf_inputs* inputs, const tg_svgf_outputs* outputs, void* stream);
 
-/* Times every (rows_per_thread, ctas_per_sm) candidate on `steps` steps of the
- * given frames, keeps the fastest, then zeroes every stream's state. */
+/* Times every candidate - strategy x rows_per_thread (x ctas_per_sm for the
+ * persistent launch) - on `steps` steps of the given frames, keeps the
+ * fastest, then zeroes every stream's state. */
 TG_API int tg_svgf_batch_autotune(tg_svgf_batch* b, uint32_t n, const uint32_t* stream_ids,
                                   const tg_svgf_inputs* inputs, const tg_svgf_outputs* outputs, uint32_t steps,
                                   void* stream);
@@ -294,8 +303,8 @@ typedef struct tg_svgf_server_desc {
     uint32_t max_batch;        /* frames per launch, 1 .. TG_SVGF_BATCH_MAX_STREAMS */
     int32_t device;            /* -1 = current */
     int32_t batching;          /* 1: continuous batching; 0: plain per-request launches */
-    int32_t use_graph;         /* batching: replay launches from CUDA graphs */
-    int32_t reserved;
+    int32_t use_graph;         /* batching with the persistent strategy: replay launches from CUDA graphs */
+    int32_t strategy;          /* batching: TG_SVGF_BATCH_STAGES (default) or TG_SVGF_BATCH_PERSISTENT */
 } tg_svgf_server_desc;
 
 typedef struct tg_svgf_request_info {

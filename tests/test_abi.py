@@ -107,6 +107,6 @@ def test_server_and_batch_reject_bad_descriptors_on_the_host():
     assert lib.tg_svgf_server_create(C.byref(d), C.byref(h)) == L.ERR_INVALID  # max_batch 0
     ws = (C.c_uint32 * 1)(16)
     hs = (C.c_uint32 * 1)(0)
-    b = L.BatchDesc(1, ws, hs, L.default_params(), 0, 0, 0, 1, 0, 0)
+    b = L.BatchDesc(1, ws, hs, L.default_params(), 0, 0, 0, 1, 0, 0, 0)
     assert lib.tg_svgf_batch_create(C.byref(b), C.byref(h)) == L.ERR_INVALID  # zero height
     assert not h.value

@@ -38,14 +38,14 @@ def _single(w, h, seq, storage, dev):
     return outs
 
 
-@pytest.mark.parametrize("batching", [True, False])
-def test_sessions_alone_equal_in_mix(cuda_dev, batching):
+@pytest.mark.parametrize("batching,strategy", [(True, 0), (True, 1), (False, 0)])
+def test_sessions_alone_equal_in_mix(cuda_dev, batching, strategy):
     """Interleaved frames of several sessions give each session the single-stream result."""
     sizes = [(64, 36), (160, 90), (33, 17)]
     frames = 4
     seqs = [_host_seq(w, h, frames, seed=3 + j, f16=True) for j, (w, h) in enumerate(sizes)]
     want = [_single(w, h, seq, tg.STORAGE_FP16, cuda_dev) for (w, h), seq in zip(sizes, seqs)]
-    sv = Server(256 << 20, max_batch=8, batching=batching, storage=tg.STORAGE_FP16)
+    sv = Server(256 << 20, max_batch=8, batching=batching, storage=tg.STORAGE_FP16, strategy=strategy)
     outs = [[torch.empty((h, w, 4), dtype=torch.float16, pin_memory=True) for _ in range(frames)] for (w, h) in sizes]
     tickets = []
     for t in range(frames):
@@ -133,7 +133,8 @@ def test_barrier_wait_runs_out_and_reports(cuda_dev):
     sc = scene.PlaneScene(scene.config1(64, 36, seed=9))
     fr = {k: v.to(cuda_dev) for k, v in sc.frame(0).items() if k in KEYS}
     out = [torch.empty((36, 64, 4), device=cuda_dev)]
-    b = Batch(sizes, storage=tg.STORAGE_FP32, barrier_timeout_us=2000, debug_barrier_extra=1)
+    b = Batch(sizes, storage=tg.STORAGE_FP32, strategy=tg._lib.BATCH_PERSISTENT, barrier_timeout_us=2000,
+              debug_barrier_extra=1)
     b.denoise([0], [fr], out)
     with pytest.raises(tg.TgError) as e:
         b.synchronize()

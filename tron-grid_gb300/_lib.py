@@ -18,6 +18,7 @@ FMT_NONE, FMT_RGBA32F, FMT_RGBA16F, FMT_R32F, FMT_RGB32F, FMT_OCT16, FMT_RG32F, 
 FMT_BYTES = {FMT_RGBA32F: 16, FMT_RGBA16F: 8, FMT_R32F: 4, FMT_RGB32F: 12, FMT_OCT16: 4, FMT_RG32F: 8, FMT_RG16F: 4}
 # tg_svgf_mode / tg_svgf_storage
 MODE_REF_EXACT, MODE_FULL = 0, 1
+BATCH_STAGES, BATCH_PERSISTENT = 0, 1
 STORAGE_FP32, STORAGE_FP16 = 0, 1
 
 
@@ -61,13 +62,13 @@ class KernelStat(C.Structure):
 class BatchDesc(C.Structure):
     _fields_ = [("n_streams", C.c_uint32), ("widths", C.POINTER(C.c_uint32)), ("heights", C.POINTER(C.c_uint32)),
                 ("params", Params), ("device", C.c_int32), ("rows_per_thread", C.c_int32),
-                ("ctas_per_sm", C.c_int32), ("use_graph", C.c_int32), ("barrier_timeout_us", C.c_uint32),
-                ("debug_barrier_extra", C.c_int32)]
+                ("ctas_per_sm", C.c_int32), ("use_graph", C.c_int32), ("strategy", C.c_int32),
+                ("barrier_timeout_us", C.c_uint32), ("debug_barrier_extra", C.c_int32)]
 
 
 class BatchInfo(C.Structure):
     _fields_ = [("n_streams", C.c_uint32), ("rows_per_thread", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("grid_ctas", C.c_int32), ("graphs", C.c_int32), ("reserved", C.c_int32),
+                ("grid_ctas", C.c_int32), ("graphs", C.c_int32), ("strategy", C.c_int32),
                 ("state_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64), ("steps", C.c_uint64),
                 ("barrier_timeouts", C.c_uint64), ("tuned_ms", C.c_double)]
 
@@ -75,7 +76,7 @@ class BatchInfo(C.Structure):
 class ServerDesc(C.Structure):
     _fields_ = [("params", Params), ("hbm_budget_bytes", C.c_uint64), ("max_sessions", C.c_uint32),
                 ("max_batch", C.c_uint32), ("device", C.c_int32), ("batching", C.c_int32),
-                ("use_graph", C.c_int32), ("reserved", C.c_int32)]
+                ("use_graph", C.c_int32), ("strategy", C.c_int32)]
 
 
 class RequestInfo(C.Structure):

@@ -13,7 +13,7 @@ class Batch:
     """N camera streams of their own resolutions, FULL mode, denoised step by step."""
 
     def __init__(self, sizes, storage: int = L.STORAGE_FP16, device: int | None = None, rows_per_thread: int = 0,
-                 ctas_per_sm: int = 0, use_graph: bool = True, barrier_timeout_us: int = 0,
+                 ctas_per_sm: int = 0, use_graph: bool = True, strategy: int = 0, barrier_timeout_us: int = 0,
                  debug_barrier_extra: int = 0, **params):
         self.lib = L.load()
         self.sizes = [(int(w), int(h)) for (w, h) in sizes]
@@ -23,7 +23,7 @@ class Batch:
         if device is None:
             device = torch.cuda.current_device()
         self.params = L.default_params(L.MODE_FULL, storage, **params)
-        d = L.BatchDesc(n, ws, hs, self.params, device, rows_per_thread, ctas_per_sm, int(use_graph),
+        d = L.BatchDesc(n, ws, hs, self.params, device, rows_per_thread, ctas_per_sm, int(use_graph), strategy,
                         barrier_timeout_us, debug_barrier_extra)
         h = C.c_void_p()
         L.check(self.lib.tg_svgf_batch_create(C.byref(d), C.byref(h)))
@@ -62,7 +62,7 @@ class Batch:
     def info(self) -> dict:
         i = L.BatchInfo()
         L.check(self.lib.tg_svgf_batch_get_info(self.handle, C.byref(i)))
-        return {k: getattr(i, k) for k, _ in L.BatchInfo._fields_ if k != "reserved"}
+        return {k: getattr(i, k) for k, _ in L.BatchInfo._fields_}
 
     def close(self):
         if getattr(self, "handle", None):

@@ -61,6 +61,9 @@ struct tg_svgf_batch {
     int sm_count = 0;
     long long spin_cycles = kBarrierSpinCycles;
     int barrier_extra = 0;
+    int strategy = TG_SVGF_BATCH_STAGES;
+    std::vector<int> grids[2];  // per-stage grid of the step in table buffer k
+    std::vector<int> sig[2];    // grids the graph of buffer k was captured with
 };
 
 namespace {
@@ -107,8 +110,9 @@ void drop_graphs(tg_svgf_batch* b)
         }
 }
 
-int set_config(tg_svgf_batch* b, int R, int ctas)
+int set_config(tg_svgf_batch* b, int strategy, int R, int ctas)
 {
+    b->strategy = strategy;
     const bool f16 = b->p.storage == TG_SVGF_STORAGE_FP16;
     const int lim = max_ctas_per_sm(f16, R);
     if (lim < 1) return fail(TG_ERR_CUDA, "persistent kernel cannot be resident (occupancy query failed)");
@@ -120,8 +124,43 @@ int set_config(tg_svgf_batch* b, int R, int ctas)
     return TG_OK;
 }
 
+using PixFn = void (*)(const char*, int);
+using LevFn = void (*)(const char*, int, int);
+
+PixFn pixel_kernel(bool f16, int stage)
+{
+    if (f16) return stage == 0 ? k_ms_pixel<ST_FP16, 0> : k_ms_pixel<ST_FP16, 1>;
+    return stage == 0 ? k_ms_pixel<ST_FP32, 0> : k_ms_pixel<ST_FP32, 1>;
+}
+
+LevFn level_kernel(bool f16, int R)
+{
+    if (f16) return R == 1 ? k_ms_level<ST_FP16, 1> : k_ms_level<ST_FP16, 2>;
+    return R == 1 ? k_ms_level<ST_FP32, 1> : k_ms_level<ST_FP32, 2>;
+}
+
+// One launch per stage over the work table of buffer k.
+cudaError_t launch_stages(tg_svgf_batch* b, int k, cudaStream_t s)
+{
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(b->d_table[k], b->h_table[k], b->tbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return e;
+    const bool f16 = b->p.storage == TG_SVGF_STORAGE_FP16;
+    const std::vector<int>& g = b->grids[k];
+    for (size_t st = 0; st < g.size(); ++st) {
+        if (g[st] <= 0) continue;
+        if (st < 2)
+            pixel_kernel(f16, int(st))<<<g[st], dim3(kBlockX, kBlockY), 0, s>>>(b->d_table[k], b->cap);
+        else
+            level_kernel(f16, b->R)<<<g[st], dim3(kLvTX, kLvRows), 0, s>>>(b->d_table[k], b->cap, int(st) - 2);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_step(tg_svgf_batch* b, int k, cudaStream_t s)
 {
+    if (b->strategy == TG_SVGF_BATCH_STAGES) return launch_stages(b, k, s);
     cudaError_t e;
     if ((e = cudaMemsetAsync(b->d_bar, 0, sizeof(BarrierState), s)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(b->d_table[k], b->h_table[k], b->tbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
@@ -151,7 +190,13 @@ cudaError_t launch_step(tg_svgf_batch* b, int k, cudaStream_t s)
 // falls back to direct launches.
 void capture(tg_svgf_batch* b, int k)
 {
-    if (!b->use_graph || !b->graphs_ok || b->exec[k]) return;
+    if (!b->use_graph || !b->graphs_ok) return;
+    if (b->exec[k] && b->sig[k] == b->grids[k]) return;
+    if (b->exec[k]) {
+        cudaGraphExecDestroy(b->exec[k]);
+        b->exec[k] = nullptr;
+    }
+    b->sig[k] = b->grids[k];
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
         cudaGetLastError();
@@ -196,6 +241,7 @@ void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const 
     hd->n_stages = 2 + b->p.levels;
     int* prefix = reinterpret_cast<int*>(t + table_prefix_offset());
     BatchEntry* ent = reinterpret_cast<BatchEntry*>(t + table_entries_offset(b->cap));
+    b->grids[k].assign(hd->n_stages, 0);
     for (int stage = 0; stage < hd->n_stages; ++stage) {
         int* pf = prefix + stage * (b->cap + 1);
         int acc = 0;
@@ -208,6 +254,7 @@ void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const 
                 acc += int(level_blocks(level_geom(W, H, 1 << (stage - 2), b->R)));
         }
         pf[n] = acc;
+        b->grids[k][stage] = acc;
     }
     for (uint32_t j = 0; j < n; ++j) {
         tg_svgf_batch::Stream& s = b->st[ids[j]];
@@ -401,7 +448,9 @@ int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
     b->h_err[0] = b->h_err[1] = 0;
     if (cudaMemset(b->d_bar, 0, sizeof(BarrierState)) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
         return cleanup(fail(TG_ERR_CUDA, "batch initialisation failed"));
-    st = set_config(b, d->rows_per_thread ? d->rows_per_thread : 2, d->ctas_per_sm);
+    if (d->strategy != TG_SVGF_BATCH_STAGES && d->strategy != TG_SVGF_BATCH_PERSISTENT)
+        return cleanup(fail(TG_ERR_INVALID, "strategy %d unknown", d->strategy));
+    st = set_config(b, d->strategy, d->rows_per_thread ? d->rows_per_thread : 2, d->ctas_per_sm);
     if (st) return cleanup(st);
     *out = b;
     return TG_OK;
@@ -447,30 +496,32 @@ int tg_svgf_batch_autotune(tg_svgf_batch* b, uint32_t n, const uint32_t* ids, co
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return fail(TG_ERR_CUDA, "event creation failed");
     double best = 1e30;
-    int bestR = b->R, bestC = b->ctas;
-    for (int R = 1; R <= 2; ++R) {
-        const int lim = max_ctas_per_sm(f16, R);
-        for (int c = 1; c <= lim; ++c) {
-            if ((st = set_config(b, R, c))) break;
-            if ((st = run_step(b, n, ids, in, out, stream)) != TG_OK) break;  // warm-up, also captures
-            if ((st = run_step(b, n, ids, in, out, stream)) != TG_OK) break;
-            cudaEventRecord(e0, stream);
-            for (uint32_t k = 0; k < steps && st == TG_OK; ++k) st = run_step(b, n, ids, in, out, stream);
-            cudaEventRecord(e1, stream);
-            if (st) break;
-            if (cudaEventSynchronize(e1) != cudaSuccess) {
-                st = fail(TG_ERR_CUDA, "autotune step failed");
-                break;
-            }
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms / steps < best) {
-                best = ms / steps;
-                bestR = R;
-                bestC = c;
-            }
-        }
+    int bestR = b->R, bestC = b->ctas, bestS = b->strategy;
+    for (int cand = 0; cand < 2 * (1 + 3) && st == TG_OK; ++cand) {
+        // candidates: (stages, R) for R = 1, 2, then (persistent, R, ctas) up to the occupancy limit
+        const int strat = cand < 2 ? TG_SVGF_BATCH_STAGES : TG_SVGF_BATCH_PERSISTENT;
+        const int R = cand < 2 ? cand + 1 : 1 + (cand - 2) / 3;
+        const int c = cand < 2 ? 0 : 1 + (cand - 2) % 3;
+        if (strat == TG_SVGF_BATCH_PERSISTENT && c > max_ctas_per_sm(f16, R)) continue;
+        if ((st = set_config(b, strat, R, c))) break;
+        if ((st = run_step(b, n, ids, in, out, stream)) != TG_OK) break;  // warm-up, also captures
+        if ((st = run_step(b, n, ids, in, out, stream)) != TG_OK) break;
+        cudaEventRecord(e0, stream);
+        for (uint32_t k = 0; k < steps && st == TG_OK; ++k) st = run_step(b, n, ids, in, out, stream);
+        cudaEventRecord(e1, stream);
         if (st) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            st = fail(TG_ERR_CUDA, "autotune step failed");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms / steps < best) {
+            best = ms / steps;
+            bestR = R;
+            bestC = c;
+            bestS = strat;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -479,7 +530,7 @@ int tg_svgf_batch_autotune(tg_svgf_batch* b, uint32_t n, const uint32_t* ids, co
         if (!st) st = r;
     }
     if (st) return st;
-    if ((st = set_config(b, bestR, bestC))) return st;
+    if ((st = set_config(b, bestS, bestR, bestC))) return st;
     b->tuned_ms = best;
     // tuning advanced every stream: zero all state
     for (auto& s : b->st) {
@@ -523,6 +574,7 @@ int tg_svgf_batch_get_info(const tg_svgf_batch* b, tg_svgf_batch_info* info)
     info->ctas_per_sm = b->ctas;
     info->grid_ctas = b->grid;
     info->graphs = (b->use_graph && b->graphs_ok) ? 1 : 0;
+    info->strategy = b->strategy;
     info->state_bytes = b->state_bytes;
     info->scratch_bytes = b->scratch_bytes;
     info->steps = b->steps;

@@ -135,4 +135,63 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
     }
 }
 
+// ------------------------------------------------------------------------
+// Stage kernels over the same work table: one launch per stage for all the
+// active streams (the work-list of one stage is the blocks of one grid).  The
+// hardware schedules the blocks; each kernel keeps its own occupancy.
+
+__device__ __forceinline__ int find_stream(const int* pf, int n, int item)
+{
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pf[mid] <= item)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+template <int ST, int STAGE>
+__global__ void __launch_bounds__(kBlockX* kBlockY) k_ms_pixel(const char* __restrict__ table, int cap)
+{
+    const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
+    const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + STAGE * (cap + 1);
+    const int item = blockIdx.x;
+    if (item >= pf[hd->n]) return;
+    const int j = find_stream(pf, hd->n, item);
+    const int local = item - pf[j];
+    const FullArgs& a = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap))[j].fa;
+    const int tx = (a.w + kBlockX - 1) / kBlockX;
+    const int x = (local % tx) * kBlockX + threadIdx.x;
+    const int y = (local / tx) * kBlockY + threadIdx.y;
+    if (x >= a.w || y >= a.h) return;
+    if (STAGE == 0)
+        full_temporal_px<ST>(a, x, y);
+    else
+        full_variance_px<ST>(a, x, y);
+}
+
+template <int ST, int R>
+__global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_ms_level(const char* __restrict__ table, int cap, int L)
+{
+    __shared__ LevelSmem<R> sm;
+    const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
+    const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
+    const int item = blockIdx.x;
+    if (item >= pf[hd->n]) return;
+    const int j = find_stream(pf, hd->n, item);
+    const BatchEntry& e = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap))[j];
+    const FullArgs& a = e.fa;
+    LevelArgs lv;
+    lv.col_src = (L & 1) ? e.colB : e.colA;
+    lv.col_dst = (L & 1) ? e.colA : e.colB;
+    lv.level = L;
+    lv.last = L == hd->levels - 1;
+    lv.lin = res_layout(a.w, a.h, L);
+    lv.lout = res_layout(a.w, a.h, L + 1);
+    full_level_tile<ST, R>(a, lv, level_geom(a.w, a.h, 1 << L, R), item - pf[j], sm);
+}
+
 } // namespace tg

@@ -321,6 +321,27 @@ cudaError_t enqueue_persistent(tg_svgf_server* sv, int k, cudaStream_t st)
     return cudaMemcpyAsync(sv->h_err + k, &sv->d_bar->err, sizeof(int), cudaMemcpyDeviceToHost, st);
 }
 
+void launch_stage_kernels(tg_svgf_server* sv, int k, const std::vector<int>& grids)
+{
+    cudaStream_t st = sv->s_comp;
+    cudaMemcpyAsync(sv->d_table[k], sv->h_table[k], sv->tbytes, cudaMemcpyHostToDevice, st);
+    for (size_t g = 0; g < grids.size(); ++g) {
+        if (grids[g] <= 0) continue;
+        if (g < 2) {
+            if (sv->f16)
+                (g == 0 ? k_ms_pixel<ST_FP16, 0> : k_ms_pixel<ST_FP16, 1>)<<<grids[g], dim3(kBlockX, kBlockY), 0, st>>>(
+                    sv->d_table[k], sv->cap);
+            else
+                (g == 0 ? k_ms_pixel<ST_FP32, 0> : k_ms_pixel<ST_FP32, 1>)<<<grids[g], dim3(kBlockX, kBlockY), 0, st>>>(
+                    sv->d_table[k], sv->cap);
+        } else if (sv->f16) {
+            k_ms_level<ST_FP16, kR><<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, int(g) - 2);
+        } else {
+            k_ms_level<ST_FP32, kR><<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, int(g) - 2);
+        }
+    }
+}
+
 void launch_batch(tg_svgf_server* sv, std::vector<Sess*>& ss, int k)
 {
     char* t = sv->h_table[k];
@@ -332,6 +353,7 @@ void launch_batch(tg_svgf_server* sv, std::vector<Sess*>& ss, int k)
     hd->n_stages = 2 + hd->levels;
     int* prefix = reinterpret_cast<int*>(t + table_prefix_offset());
     BatchEntry* ent = reinterpret_cast<BatchEntry*>(t + table_entries_offset(sv->cap));
+    std::vector<int> grids(hd->n_stages, 0);
     for (int stage = 0; stage < hd->n_stages; ++stage) {
         int* pf = prefix + stage * (sv->cap + 1);
         int acc = 0;
@@ -344,11 +366,16 @@ void launch_batch(tg_svgf_server* sv, std::vector<Sess*>& ss, int k)
                 acc += int(level_blocks(level_geom(W, H, 1 << (stage - 2), kR)));
         }
         pf[n] = acc;
+        grids[stage] = acc;
     }
     for (int j = 0; j < n; ++j) {
         ent[j].fa = args_for(sv, *ss[j]);
         ent[j].colA = ss[j]->colA;
         ent[j].colB = ss[j]->colB;
+    }
+    if (sv->d.strategy == TG_SVGF_BATCH_STAGES) {
+        launch_stage_kernels(sv, k, grids);
+        return;
     }
     if (sv->d.use_graph && sv->graphs_ok && !sv->exec[k]) {
         cudaGraph_t g = nullptr;
@@ -522,7 +549,7 @@ void scheduler(tg_svgf_server* sv)
         for (Sess* s : fresh) cudaMemsetAsync(s->state, 0, s->state_len, sv->s_comp);
         Flight* fl = new Flight();
         fl->reqs = batch;
-        fl->table_k = sv->d.batching ? k : -1;
+        fl->table_k = (sv->d.batching && sv->d.strategy == TG_SVGF_BATCH_PERSISTENT) ? k : -1;
         cudaEventCreateWithFlags(&fl->ev_comp, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&fl->ev_d2h, cudaEventDisableTiming);
         const Clock::time_point tl = Clock::now();
@@ -661,6 +688,8 @@ int tg_svgf_server_create(const tg_svgf_server_desc* d, tg_svgf_server** out)
         cudaStreamCreateWithFlags(&sv->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&sv->ev_h2d, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(TG_ERR_CUDA, "stream creation failed"));
+    if (d->strategy != TG_SVGF_BATCH_STAGES && d->strategy != TG_SVGF_BATCH_PERSISTENT)
+        return bail(fail(TG_ERR_INVALID, "strategy %d unknown", d->strategy));
     if (d->batching) {
         int coop = 0;
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);

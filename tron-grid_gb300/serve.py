@@ -13,13 +13,14 @@ class Server:
     """Sessions submit frames (host tensors, ideally pinned); results land in the given host outputs."""
 
     def __init__(self, budget_bytes: int, max_sessions: int = 1024, max_batch: int = 64, batching: bool = True,
-                 storage: int = L.STORAGE_FP16, device: int | None = None, use_graph: bool = True, **params):
+                 storage: int = L.STORAGE_FP16, device: int | None = None, use_graph: bool = True,
+                 strategy: int = 0, **params):
         self.lib = L.load()
         if device is None:
             device = torch.cuda.current_device()
         self.params = L.default_params(L.MODE_FULL, storage, **params)
         d = L.ServerDesc(self.params, int(budget_bytes), max_sessions, max_batch, device, int(batching),
-                         int(use_graph), 0)
+                         int(use_graph), strategy)
         h = C.c_void_p()
         L.check(self.lib.tg_svgf_server_create(C.byref(d), C.byref(h)))
         self.handle = h
