@@ -305,6 +305,9 @@ typedef struct tg_svgf_server_desc {
     int32_t batching;          /* 1: continuous batching; 0: plain per-request launches */
     int32_t use_graph;         /* batching with the persistent strategy: replay launches from CUDA graphs */
     int32_t strategy;          /* batching: TG_SVGF_BATCH_STAGES (default) or TG_SVGF_BATCH_PERSISTENT */
+    uint64_t max_batch_pixels; /* batching: stop adding frames to a launch past this many pixels (the
+                                  first frame is always taken); bounds a launch's duration and so the
+                                  wait of the frames queued behind it.  0 = 4 Mpx */
 } tg_svgf_server_desc;
 
 typedef struct tg_svgf_request_info {

@@ -101,9 +101,9 @@ def test_cpp_wrapper_compiles(tmp_path):
 def test_server_and_batch_reject_bad_descriptors_on_the_host():
     lib = L.load()
     h = C.c_void_p()
-    d = L.ServerDesc(L.default_params(L.MODE_REF_EXACT), 1 << 30, 16, 8, 0, 1, 1, 0)
+    d = L.ServerDesc(L.default_params(L.MODE_REF_EXACT), 1 << 30, 16, 8, 0, 1, 1, 0, 0)
     assert lib.tg_svgf_server_create(C.byref(d), C.byref(h)) == L.ERR_INVALID  # REF_EXACT not served
-    d = L.ServerDesc(L.default_params(), 1 << 30, 16, 0, 0, 1, 1, 0)
+    d = L.ServerDesc(L.default_params(), 1 << 30, 16, 0, 0, 1, 1, 0, 0)
     assert lib.tg_svgf_server_create(C.byref(d), C.byref(h)) == L.ERR_INVALID  # max_batch 0
     ws = (C.c_uint32 * 1)(16)
     hs = (C.c_uint32 * 1)(0)

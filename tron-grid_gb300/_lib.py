@@ -76,7 +76,7 @@ class BatchInfo(C.Structure):
 class ServerDesc(C.Structure):
     _fields_ = [("params", Params), ("hbm_budget_bytes", C.c_uint64), ("max_sessions", C.c_uint32),
                 ("max_batch", C.c_uint32), ("device", C.c_int32), ("batching", C.c_int32),
-                ("use_graph", C.c_int32), ("strategy", C.c_int32)]
+                ("use_graph", C.c_int32), ("strategy", C.c_int32), ("max_batch_pixels", C.c_uint64)]
 
 
 class RequestInfo(C.Structure):

@@ -464,6 +464,8 @@ void scheduler(tg_svgf_server* sv)
             if (sv->stop && sv->queue.empty()) break;
             std::vector<uint64_t> busy;
             const uint32_t maxb = sv->d.batching ? sv->d.max_batch : 1u;
+            const uint64_t max_px = sv->d.max_batch_pixels ? sv->d.max_batch_pixels : (uint64_t(4) << 20);
+            uint64_t batch_px = 0;
             const Clock::time_point now = Clock::now();
             for (auto it = sv->queue.begin(); it != sv->queue.end() && batch.size() < maxb;) {
                 Req* r = *it;
@@ -482,6 +484,7 @@ void scheduler(tg_svgf_server* sv)
                     ++it;
                     continue;
                 }
+                if (!batch.empty() && batch_px + uint64_t(r->w) * r->h > max_px) break;
                 // a frame of another size or format restarts the session
                 const int f[5] = {r->in.radiance.format, r->in.depth.format, r->in.normal.format, r->in.motion.format,
                                   r->out.denoised.format};
@@ -514,6 +517,7 @@ void scheduler(tg_svgf_server* sv)
                 if (s.fresh) fresh.push_back(&s);
                 s.fresh = false;
                 busy.push_back(s.id);
+                batch_px += uint64_t(r->w) * r->h;
                 batch.push_back(r);
                 ss.push_back(&s);
                 it = sv->queue.erase(it);

@@ -14,13 +14,13 @@ class Server:
 
     def __init__(self, budget_bytes: int, max_sessions: int = 1024, max_batch: int = 64, batching: bool = True,
                  storage: int = L.STORAGE_FP16, device: int | None = None, use_graph: bool = True,
-                 strategy: int = 0, **params):
+                 strategy: int = 0, max_batch_pixels: int = 0, **params):
         self.lib = L.load()
         if device is None:
             device = torch.cuda.current_device()
         self.params = L.default_params(L.MODE_FULL, storage, **params)
         d = L.ServerDesc(self.params, int(budget_bytes), max_sessions, max_batch, device, int(batching),
-                         int(use_graph), strategy)
+                         int(use_graph), strategy, int(max_batch_pixels))
         h = C.c_void_p()
         L.check(self.lib.tg_svgf_server_create(C.byref(d), C.byref(h)))
         self.handle = h
