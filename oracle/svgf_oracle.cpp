@@ -110,15 +110,60 @@ inline void oct16_decode(int16_t ex, int16_t ey, float& nx, float& ny, float& nz
     nz = vz * inv;
 }
 
+// Unnormalised octahedral decode: the point on the unit octahedron.  The
+// FP16 storage form keeps normals this way; the reprojection normal test is
+// scale-free, and the edge-stopping weights normalise on use.
+inline void oct16_decode_raw(int16_t ex, int16_t ey, float& nx, float& ny, float& nz)
+{
+    const float kInv = 1.0f / 32767.0f;
+    float px = std::max(-1.0f, static_cast<float>(ex) * kInv);
+    float py = std::max(-1.0f, static_cast<float>(ey) * kInv);
+    float vz = 1.0f - std::fabs(px) - std::fabs(py);
+    if (vz < 0.0f) {
+        float ox = (1.0f - std::fabs(py)) * sgn_nz(px);
+        float oy = (1.0f - std::fabs(px)) * sgn_nz(py);
+        px = ox;
+        py = oy;
+    }
+    nx = px;
+    ny = py;
+    nz = vz;
+}
+
 template <class T> inline void oct16_roundtrip(T& x, T& y, T& z)
 {
     int16_t ex, ey;
     oct16_encode(float(x), float(y), float(z), ex, ey);
     float a, b, c;
-    oct16_decode(ex, ey, a, b, c);
+    oct16_decode_raw(ex, ey, a, b, c);
     x = T(a);
     y = T(b);
     z = T(c);
+}
+
+// Reprojection normal test, scale-free: the angle between a and b is at most
+// acos(0.9) iff a.b >= 0 and (a.b)^2 >= 0.81 |a|^2 |b|^2.
+template <class T> inline bool normal_close(T ax, T ay, T az, T bx, T by, T bz)
+{
+    T d = ax * bx + ay * by + az * bz;
+    if (!(d >= T(0))) return false;
+    T aa = ax * ax + ay * ay + az * az;
+    T bb = bx * bx + by * by + bz * bz;
+    return d * d >= (T(0.81f) * aa) * bb;
+}
+
+// The unit normal used by the edge-stopping weights.
+template <class T> inline void unit_normal(const T* g, bool f16, T& x, T& y, T& z)
+{
+    x = g[0];
+    y = g[1];
+    z = g[2];
+    if (f16) {
+        T inv = T(1) / std::sqrt(x * x + y * y + z * z);
+        x *= inv;
+        y *= inv;
+        z *= inv;
+    }
 }
 
 inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
@@ -280,7 +325,7 @@ constexpr float kEpsZ = 1e-3f;         // depth edge-stop denominator floor (met
 constexpr float kDepthRel = 0.05f;     // reprojection depth test: relative term
 constexpr float kDepthGrad = 4.0f;     // reprojection depth test: gradient term
 constexpr float kDepthAbs = 0.1f;      // reprojection depth test: absolute term
-constexpr float kNormalCos = 0.9f;     // reprojection normal test: min cosine
+constexpr float kNormalCos = 0.9f;     // reprojection normal test: min cosine (tested squared, 0.81)
 constexpr float kB3[5] = {1.0f / 16.0f, 1.0f / 4.0f, 3.0f / 8.0f, 1.0f / 4.0f, 1.0f / 16.0f};
 constexpr float kG3[3] = {0.25f, 0.5f, 0.25f};
 
@@ -393,8 +438,8 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                 if (!(len_t > T(0))) continue;
                 T zt = guide_prev[4 * j + 3];
                 if (!(std::fabs(zt - z) <= ztol)) continue;
-                T d = guide_prev[4 * j + 0] * nx + guide_prev[4 * j + 1] * ny + guide_prev[4 * j + 2] * nz;
-                if (!(d >= T(kNormalCos))) continue;
+                if (!normal_close(guide_prev[4 * j + 0], guide_prev[4 * j + 1], guide_prev[4 * j + 2], nx, ny, nz))
+                    continue;
                 ok[k] = true;
                 sw += bw[k];
                 hr += bw[k] * hist_prev[4 * j + 0];
@@ -455,7 +500,9 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
             int len = int(B.tc[4 * i + 3]);
             T var;
             if (len < P.fallback_frames) {
-                T nx = guide_cur[4 * i + 0], ny = guide_cur[4 * i + 1], nz = guide_cur[4 * i + 2], z = guide_cur[4 * i + 3];
+                T nx, ny, nz;
+                unit_normal(guide_cur + 4 * i, f16, nx, ny, nz);
+                T z = guide_cur[4 * i + 3];
                 T gx = B.gx[i], gy = B.gy[i];
                 T mup = mom_cur[2 * i + 0];
                 T s0 = 0, s1 = 0, s2 = 0;
@@ -466,7 +513,9 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                         int qx = x + dx;
                         if (qx < 0 || qx >= w) continue;
                         size_t j = size_t(qy) * w + qx;
-                        T d = guide_cur[4 * j + 0] * nx + guide_cur[4 * j + 1] * ny + guide_cur[4 * j + 2] * nz;
+                        T qx_, qy_, qz_;
+                        unit_normal(guide_cur + 4 * j, f16, qx_, qy_, qz_);
+                        T d = qx_ * nx + qy_ * ny + qz_ * nz;
                         T wn = normal_weight(d, P.sigma_n);
                         if (!(wn > T(0))) continue;
                         T den = sz * std::fabs(T(dx) * gx + T(dy) * gy) + T(kEpsZ);
@@ -507,7 +556,9 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                 size_t i = size_t(y) * w + x;
                 T cr = src[4 * i + 0], cg = src[4 * i + 1], cb = src[4 * i + 2], cv = src[4 * i + 3];
                 T cl = lum(cr, cg, cb);
-                T nx = guide_cur[4 * i + 0], ny = guide_cur[4 * i + 1], nz = guide_cur[4 * i + 2], z = guide_cur[4 * i + 3];
+                T nx, ny, nz;
+                unit_normal(guide_cur + 4 * i, f16, nx, ny, nz);
+                T z = guide_cur[4 * i + 3];
                 T gx = B.gx[i], gy = B.gy[i];
                 // 3x3 Gaussian of the variance around the centre (inside taps only).
                 T gv = 0, gw = 0;
@@ -532,7 +583,9 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                         int qx = x + dx * s;
                         if (qx < 0 || qx >= w) continue;
                         size_t j = size_t(qy) * w + qx;
-                        T d = guide_cur[4 * j + 0] * nx + guide_cur[4 * j + 1] * ny + guide_cur[4 * j + 2] * nz;
+                        T ux, uy, uz;
+                        unit_normal(guide_cur + 4 * j, f16, ux, uy, uz);
+                        T d = ux * nx + uy * ny + uz * nz;
                         T wn = normal_weight(d, P.sigma_n);
                         if (!(wn > T(0))) continue;
                         T qr = src[4 * j + 0], qg = src[4 * j + 1], qb = src[4 * j + 2], qv = src[4 * j + 3];

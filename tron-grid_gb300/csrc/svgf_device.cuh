@@ -30,7 +30,7 @@ constexpr float kEpsZ = 1e-3f;     // depth edge-stop denominator floor (metres)
 constexpr float kDepthRel = 0.05f; // reprojection depth test: relative term
 constexpr float kDepthGrad = 4.0f; // reprojection depth test: gradient term
 constexpr float kDepthAbs = 0.1f;  // reprojection depth test: absolute term
-constexpr float kNormalCos = 0.9f; // reprojection normal test: minimum cosine
+constexpr float kNormalCos = 0.9f; // reprojection normal test: minimum cosine (tested squared: 0.81)
 constexpr float kHalfMax = 65504.0f;
 constexpr float kLog2eF = 1.4426950408889634f;
 
@@ -142,6 +142,35 @@ __device__ __forceinline__ float3 oct16_decode(uint32_t u)
     return make_float3(__fmul_rn(px, inv), __fmul_rn(py, inv), __fmul_rn(vz, inv));
 }
 
+// Unnormalised octahedral decode (the point on the unit octahedron), the form
+// in which FP16 storage keeps normals for the reprojection test.  Same
+// operations as the CPU oracle, so the test decides identically.
+__device__ __forceinline__ float3 oct16_decode_raw(uint32_t u)
+{
+    const float kInv = 1.0f / 32767.0f;
+    float px = fmaxf(-1.0f, __fmul_rn(float(int(int16_t(u & 0xffffu))), kInv));
+    float py = fmaxf(-1.0f, __fmul_rn(float(int(int16_t(u >> 16))), kInv));
+    const float vz = __fsub_rn(__fsub_rn(1.0f, fabsf(px)), fabsf(py));
+    if (vz < 0.0f) {
+        const float ox = __fmul_rn(__fsub_rn(1.0f, fabsf(py)), sgn_nz(px));
+        const float oy = __fmul_rn(__fsub_rn(1.0f, fabsf(px)), sgn_nz(py));
+        px = ox;
+        py = oy;
+    }
+    return make_float3(px, py, vz);
+}
+
+// Reprojection normal test, scale-free: the angle between a and b is at most
+// acos(0.9) iff a.b >= 0 and (a.b)^2 >= 0.81 |a|^2 |b|^2 (unfused, as on the CPU).
+__device__ __forceinline__ bool normal_close(float ax, float ay, float az, float bx, float by, float bz)
+{
+    const float d = dot3_rn(ax, ay, az, bx, by, bz);
+    if (!(d >= 0.0f)) return false;
+    const float aa = dot3_rn(ax, ay, az, ax, ay, az);
+    const float bb = dot3_rn(bx, by, bz, bx, by, bz);
+    return __fmul_rn(d, d) >= __fmul_rn(__fmul_rn(0.81f, aa), bb);
+}
+
 // Octahedral decode for edge-stopping weights only (never for a discrete
 // decision): reciprocal-multiply and rsqrt instead of IEEE divisions.
 __device__ __forceinline__ float3 oct16_decode_fast(uint32_t u)
@@ -193,6 +222,7 @@ __device__ __forceinline__ float3 ld_normal(const Img& im, int x, int y, bool wa
     const char* r = row_ptr(im, y);
     if (im.fmt == TG_FMT_OCT16) {
         enc = __ldg(reinterpret_cast<const uint32_t*>(r) + x);
+        if (want_enc) return make_float3(0.f, 0.f, 0.f);  // the caller decodes the code itself
         return oct16_decode(enc);
     }
     float3 n;
@@ -230,7 +260,7 @@ template <> struct Stor<ST_FP32> {
     typedef float4 guide_t;
     typedef float4 c4_t;
     typedef float2 mom_t;
-    __device__ static float4 ld_guide(const guide_t* p, size_t i) { return __ldg(p + i); }
+    __device__ static float4 ld_guide_raw(const guide_t* p, size_t i) { return __ldg(p + i); }
     __device__ static float4 ld_guide_w(const guide_t* p, size_t i) { return __ldg(p + i); }
     __device__ static float ld_guide_z(const guide_t* p, size_t i) { return __ldg(reinterpret_cast<const float*>(p + i) + 3); }
     __device__ static guide_t mk_guide(float3 n, uint32_t, float z) { return make_float4(n.x, n.y, n.z, z); }
@@ -247,10 +277,11 @@ template <> struct Stor<ST_FP16> {
     typedef uint2 guide_t;
     typedef uint2 c4_t;
     typedef uint32_t mom_t;
-    __device__ static float4 ld_guide(const guide_t* p, size_t i)
+    // guide for the reprojection test: unnormalised octahedral normal
+    __device__ static float4 ld_guide_raw(const guide_t* p, size_t i)
     {
         uint2 u = __ldg(p + i);
-        float3 n = oct16_decode(u.x);
+        float3 n = oct16_decode_raw(u.x);
         return make_float4(n.x, n.y, n.z, __uint_as_float(u.y));
     }
     // guide for edge-stopping weights (fast decode)

@@ -116,7 +116,7 @@ template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArg
 
     uint32_t enc = 0;
     float3 n = ld_normal(a.normal, x, y, ST == ST_FP16, enc);
-    if (ST == ST_FP16 && a.normal.fmt != TG_FMT_OCT16) n = oct16_decode(enc);
+    if (ST == ST_FP16) n = oct16_decode_raw(enc);  // FP16 storage keeps the octahedral code
     const float z = ld_depth(a.depth, x, y);
     static_cast<G*>(a.guide_cur)[i] = S::mk_guide(n, enc, z);
 
@@ -156,10 +156,9 @@ template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArg
         const size_t j = size_t(ty) * a.w + tx;
         const float4 hv = S::ld4(hp, j);
         if (!(hv.w > 0.0f)) continue;
-        const float4 g = S::ld_guide(gp, j);
+        const float4 g = S::ld_guide_raw(gp, j);
         if (!(fabsf(__fsub_rn(g.w, z)) <= ztol)) continue;
-        const float d = dot3_rn(g.x, g.y, g.z, n.x, n.y, n.z);
-        if (!(d >= kNormalCos)) continue;
+        if (!normal_close(g.x, g.y, g.z, n.x, n.y, n.z)) continue;
         const float2 m = S::ldm(mp, j);
         tw[k] = bw[k];
         tmu[k] = m.x;
@@ -226,7 +225,7 @@ template <int ST> __device__ __forceinline__ void full_variance_px(const FullArg
     const float2 mom = S::ldm(mc, i);
     float var = mom.y;
     if (len < a.fallback_frames) {
-        const float4 g = S::ld_guide(gc, i);
+        const float4 g = S::ld_guide_w(gc, i);
         const float2 gr = a.grad[i];
         // w = max(0, n.n')^sigma_n exp(-|dz| / (sigma_z |grad z . off| + eps_z)), as one ex2
         const float A_ = a.sigma_z * gr.x * (1.0f / kLog2eF), B_ = a.sigma_z * gr.y * (1.0f / kLog2eF);
@@ -240,7 +239,7 @@ template <int ST> __device__ __forceinline__ void full_variance_px(const FullArg
                 const int qx = x + dx;
                 if (qx < 0 || qx >= a.w) continue;
                 const size_t j = size_t(qy) * a.w + qx;
-                const float4 q = S::ld_guide(gc, j);
+                const float4 q = S::ld_guide_w(gc, j);
                 const float d = fmaf(q.z, g.z, fmaf(q.y, g.y, q.x * g.x));
                 float t = -fabsf(q.w - g.w) * rcp_approx(fabsf(float(dx) * A_ + float(dy) * B_) + ez);
                 t = fmaf(a.sigma_n, lg2_approx(fmaxf(d, 0.0f)), t);
