@@ -143,32 +143,46 @@ template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArg
     const G* gp = static_cast<const G*>(a.guide_prev);
     const C4* hp = static_cast<const C4*>(a.hist_prev);
     const M* mp = static_cast<const M*>(a.mom_prev);
+    // All four taps' history, guide and moments are loaded before any of them
+    // is tested, so the gathers overlap instead of forming a dependent chain.
+    size_t tj[4];
+    bool tin[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int tx = x0 + (k & 1), ty = y0 + (k >> 1);
+        tin[k] = tx >= 0 && ty >= 0 && tx < a.w && ty < a.h;
+        tj[k] = tin[k] ? size_t(ty) * a.w + tx : 0;
+    }
+    float4 thv[4], tg[4];
+    float2 tm[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (tin[k]) {
+            thv[k] = S::ld4(hp, tj[k]);
+            tg[k] = S::ld_guide_raw(gp, tj[k]);
+            tm[k] = S::ldm(mp, tj[k]);
+        } else {
+            thv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            tg[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            tm[k] = make_float2(0.f, 0.f);
+        }
+    }
     float sw = 0.0f, hr_ = 0.0f, hg = 0.0f, hb = 0.0f, hmu = 0.0f;
-    float tmu[4], tvar[4], tw[4];
+    float tw[4];
     int lmax = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         tw[k] = 0.0f;
-        tmu[k] = 0.0f;
-        tvar[k] = 0.0f;
-        const int tx = x0 + (k & 1), ty = y0 + (k >> 1);
-        if (tx < 0 || ty < 0 || tx >= a.w || ty >= a.h) continue;
-        const size_t j = size_t(ty) * a.w + tx;
-        const float4 hv = S::ld4(hp, j);
-        if (!(hv.w > 0.0f)) continue;
-        const float4 g = S::ld_guide_raw(gp, j);
-        if (!(fabsf(__fsub_rn(g.w, z)) <= ztol)) continue;
-        if (!normal_close(g.x, g.y, g.z, n.x, n.y, n.z)) continue;
-        const float2 m = S::ldm(mp, j);
+        if (!tin[k] || !(thv[k].w > 0.0f)) continue;
+        if (!(fabsf(__fsub_rn(tg[k].w, z)) <= ztol)) continue;
+        if (!normal_close(tg[k].x, tg[k].y, tg[k].z, n.x, n.y, n.z)) continue;
         tw[k] = bw[k];
-        tmu[k] = m.x;
-        tvar[k] = m.y;
         sw = __fadd_rn(sw, bw[k]);
-        hr_ += bw[k] * hv.x;
-        hg += bw[k] * hv.y;
-        hb += bw[k] * hv.z;
-        hmu += bw[k] * m.x;
-        lmax = max(lmax, int(hv.w));
+        hr_ += bw[k] * thv[k].x;
+        hg += bw[k] * thv[k].y;
+        hb += bw[k] * thv[k].z;
+        hmu += bw[k] * tm[k].x;
+        lmax = max(lmax, int(thv[k].w));
     }
     const float l = lum(cr, cg, cb);
     float orr, og, ob, mu, var;
@@ -182,8 +196,9 @@ template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArg
         float hvv = 0.0f;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float dm = tmu[k] - hmu;
-            hvv += tw[k] * (tvar[k] + dm * dm);
+            if (!(tw[k] > 0.0f)) continue;  // rejected taps never enter the sums
+            const float dm = tm[k].x - hmu;
+            hvv += tw[k] * (tm[k].y + dm * dm);
         }
         hvv *= inv;
         len = min(lmax + 1, a.max_history);
@@ -259,7 +274,7 @@ template <int ST> __device__ __forceinline__ void full_variance_px(const FullArg
     S::st4_sat_w(static_cast<C4*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var));
 }
 
-template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_temporal(FullArgs a)
+template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY, 4) k_full_temporal(FullArgs a)
 {
     const int x = blockIdx.x * kBlockX + threadIdx.x;
     const int y = blockIdx.y * kBlockY + threadIdx.y;
