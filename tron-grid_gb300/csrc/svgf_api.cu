@@ -193,7 +193,8 @@ struct tg_svgf {
         bool used = false;
     } stg[2];
     int stg_next = 0;
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host -> device
+    cudaStream_t d2h_stream = nullptr;   // device -> host (its own stream, so uploads never queue behind it)
     // per-kernel CUDA-event profiling
     struct Prof {
         bool on = false;
@@ -275,7 +276,9 @@ void free_staging(tg_svgf* s)
         g = tg_svgf::Staging{};
     }
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    if (s->d2h_stream) cudaStreamDestroy(s->d2h_stream);
     s->copy_stream = nullptr;
+    s->d2h_stream = nullptr;
 }
 
 int alloc_buffers(tg_svgf* s)
@@ -605,6 +608,8 @@ int tg_svgf_denoise_host(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_out
     need += align_up(size_t(fmt_bytes(out->denoised.format)) * s->w * s->h, 256);
     if (!s->copy_stream && cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(TG_ERR_CUDA, "copy stream creation failed");
+    if (!s->d2h_stream && cudaStreamCreateWithFlags(&s->d2h_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "copy stream creation failed");
     tg_svgf::Staging& sg = s->stg[s->stg_next];
     if (sg.bytes < need) {
         if (sg.buf) {
@@ -651,13 +656,13 @@ int tg_svgf_denoise_host(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_out
     dout.denoised = tg_image{sg.buf + off[4], int64_t(orow), out->denoised.format, 0};
     st = launch_frame(s, &din, &dout, stream);
     if (st) return st;
-    if (cudaEventRecord(sg.ev_comp, stream) != cudaSuccess || cudaStreamWaitEvent(s->copy_stream, sg.ev_comp, 0) != cudaSuccess)
+    if (cudaEventRecord(sg.ev_comp, stream) != cudaSuccess || cudaStreamWaitEvent(s->d2h_stream, sg.ev_comp, 0) != cudaSuccess)
         return fail(TG_ERR_CUDA, "event record failed");
     const size_t op = out->denoised.pitch_bytes ? size_t(out->denoised.pitch_bytes) : orow;
-    if (cudaMemcpy2DAsync(out->denoised.ptr, op, sg.buf + off[4], orow, orow, s->h, cudaMemcpyDeviceToHost, s->copy_stream) !=
+    if (cudaMemcpy2DAsync(out->denoised.ptr, op, sg.buf + off[4], orow, orow, s->h, cudaMemcpyDeviceToHost, s->d2h_stream) !=
         cudaSuccess)
         return fail(TG_ERR_CUDA, "output copy failed: %s", cudaGetErrorString(cudaGetLastError()));
-    if (cudaEventRecord(sg.ev_done, s->copy_stream) != cudaSuccess) return fail(TG_ERR_CUDA, "event record failed");
+    if (cudaEventRecord(sg.ev_done, s->d2h_stream) != cudaSuccess) return fail(TG_ERR_CUDA, "event record failed");
     sg.used = true;
     s->stg_next ^= 1;
     return TG_OK;
