@@ -108,12 +108,15 @@ typedef struct tg_svgf_params {
     float reserved[4];
 } tg_svgf_params;
 
+/* tg_svgf_desc.flags */
+#define TG_SVGF_FLAG_NO_TMA 1 /* stage a-trous tiles with plain loads instead of the tensor-memory accelerator */
+
 typedef struct tg_svgf_desc {
     uint32_t width;
     uint32_t height;
     tg_svgf_params params;
     int32_t device; /* CUDA device ordinal; -1 = the calling thread's current device */
-    int32_t flags;  /* 0 */
+    int32_t flags;  /* TG_SVGF_FLAG_* */
 } tg_svgf_desc;
 
 /* Per-frame inputs.  REF_EXACT reads only `radiance` (the reference's
@@ -142,6 +145,8 @@ typedef struct tg_svgf_info {
     uint64_t scratch_bytes;     /* device bytes of per-frame scratch */
     uint64_t staging_bytes;     /* device bytes of host-call staging (0 until first host call) */
     uint32_t kernels_per_frame; /* kernel launches per tg_svgf_denoise */
+    uint32_t device_errors;     /* nonzero: a bounded device-side wait gave up (results since are invalid) */
+    uint32_t tma;               /* 1: a-trous tiles are staged by the tensor-memory accelerator */
     uint32_t reserved;
 } tg_svgf_info;
 
@@ -172,7 +177,9 @@ TG_API int tg_svgf_denoise_host(tg_svgf* h, const tg_svgf_inputs* host_inputs, c
                          void* stream);
 
 /* Waits until every host copy issued by tg_svgf_denoise_host on this handle
- * has landed in host memory (the compute is ordered on the caller's stream). */
+ * has landed in host memory (the compute is ordered on the caller's stream),
+ * then reports TG_ERR_TIMEOUT if a bounded device-side wait of any earlier
+ * frame gave up. */
 TG_API int tg_svgf_synchronize(tg_svgf* h);
 
 /* Zeroes all history: the next frame is a full disocclusion (replaces the

@@ -207,3 +207,25 @@ def test_invalid_arguments_raise(cuda_dev):
     with pytest.raises(ValueError):
         d.denoise(rad.double(), dep, nrm, torch.zeros((32, 32, 2), device=cuda_dev))
     d.close()
+
+
+@pytest.mark.parametrize("storage", [tg.STORAGE_FP32, tg.STORAGE_FP16])
+def test_tma_and_plain_staging_agree(cuda_dev, storage):
+    """The a-trous tiles staged by the tensor-memory accelerator give the same bits as plain loads."""
+    W, H = 333, 197
+    f16 = storage == tg.STORAGE_FP16
+    a = tg.Denoiser(W, H, storage=storage)
+    b = tg.Denoiser(W, H, storage=storage, flags=tg._lib.FLAG_NO_TMA)
+    assert a.info()["tma"] == 1 and b.info()["tma"] == 0
+    sc = scene.PlaneScene(scene.config1(W, H, seed=12))
+    dt = torch.float16 if f16 else torch.float32
+    for t in range(6):
+        fr = sc.frame(t)
+        rad = fr["radiance"].to(dt).to(cuda_dev)
+        nrm = torch.from_numpy(oracle.oct16_encode(fr["normal"].numpy())).to(cuda_dev) if f16 else fr["normal"].to(cuda_dev)
+        args = (rad, fr["depth"].to(cuda_dev), nrm, fr["motion"].to(cuda_dev))
+        oa = a.denoise(*args, out=torch.empty((H, W, 4), dtype=dt, device=cuda_dev))
+        ob = b.denoise(*args, out=torch.empty((H, W, 4), dtype=dt, device=cuda_dev))
+        assert torch.equal(oa, ob), f"frame {t}"
+    a.synchronize()
+    assert a.info()["device_errors"] == 0

@@ -19,6 +19,7 @@ FMT_BYTES = {FMT_RGBA32F: 16, FMT_RGBA16F: 8, FMT_R32F: 4, FMT_RGB32F: 12, FMT_O
 # tg_svgf_mode / tg_svgf_storage
 MODE_REF_EXACT, MODE_FULL = 0, 1
 BATCH_STAGES, BATCH_PERSISTENT = 0, 1
+FLAG_NO_TMA = 1
 STORAGE_FP32, STORAGE_FP16 = 0, 1
 
 
@@ -51,7 +52,8 @@ class Outputs(C.Structure):
 class Info(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("frame_index", C.c_uint64),
                 ("state_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64), ("staging_bytes", C.c_uint64),
-                ("kernels_per_frame", C.c_uint32), ("reserved", C.c_uint32)]
+                ("kernels_per_frame", C.c_uint32), ("device_errors", C.c_uint32), ("tma", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class KernelStat(C.Structure):

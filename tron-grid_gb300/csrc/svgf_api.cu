@@ -97,7 +97,7 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Bytes per pixel of each handle-owned buffer.
 struct Layout {
-    size_t guide, c4, mom;
+    size_t guide, c4, mom, rec;
 };
 
 static Layout layout_of(const tg_svgf_params& p)
@@ -107,8 +107,12 @@ static Layout layout_of(const tg_svgf_params& p)
     l.guide = f16 ? 8 : 16;
     l.c4 = f16 ? 8 : 16;
     l.mom = f16 ? 4 : 8;
+    // a-trous scratch: FULL records carry the guide (32 / 16 B), REF_EXACT images do not
+    l.rec = p.mode == TG_SVGF_MODE_FULL ? (f16 ? 16 : 32) : l.c4;
     return l;
 }
+
+size_t rec_bytes_of(const tg_svgf_params& p) { return layout_of(p).rec; }
 
 size_t state_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
@@ -135,9 +139,9 @@ size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     const size_t n = size_t(w) * h;
     const Layout l = layout_of(p);
-    const size_t col = align_up(col_pixels_of(p, w, h) * l.c4, 256);
+    const size_t col = align_up(col_pixels_of(p, w, h) * l.rec, 256);
     if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * col;
-    return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256);
+    return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256) + 256;
 }
 
 int validate_params(const tg_svgf_params& p)
@@ -165,6 +169,8 @@ int validate_params(const tg_svgf_params& p)
 } // namespace tg
 
 namespace tg {
+// Output rows per thread of the tiled a-trous kernels.
+constexpr int kLevelR = 2;
 enum Family { F_REF_INIT = 0, F_REF_LEVEL, F_FULL_TEMPORAL, F_FULL_VARIANCE, F_FULL_LEVEL, kFamilies };
 static const char* kFamilyName[kFamilies] = {"ref_init", "ref_level", "full_temporal", "full_variance", "full_level"};
 } // namespace tg
@@ -185,6 +191,10 @@ struct tg_svgf {
     void* colA = nullptr;
     void* colB = nullptr;
     float2* grad = nullptr;
+    int* d_err = nullptr;  // device error word of bounded waits
+    int flags = 0;
+    bool tma = false;                // a-trous tiles staged by TMA
+    CUtensorMap tmaps[10];           // per level: the level's input records
     // host-call staging (double buffered)
     struct Staging {
         char* buf = nullptr;
@@ -244,6 +254,7 @@ void carve(tg_svgf* s)
         s->colB = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
         s->guide[0] = s->guide[1] = s->hist[0] = s->hist[1] = s->tc = nullptr;
         s->grad = nullptr;
+        s->d_err = nullptr;
     } else {
         for (int k = 0; k < 2; ++k) {
             s->guide[k] = take(n * l.guide);
@@ -252,10 +263,68 @@ void carve(tg_svgf* s)
         }
         p = s->scratch;
         s->tc = take(n * l.c4);
-        s->colA = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
-        s->colB = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
+        s->colA = take(col_pixels_of(s->p, s->w, s->h) * l.rec);
+        s->colB = take(col_pixels_of(s->p, s->w, s->h) * l.rec);
         s->grad = static_cast<float2*>(take(n * sizeof(float2)));
+        s->d_err = static_cast<int*>(take(sizeof(int)));
     }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+// One tensor map per a-trous level over that level's input records in the
+// residue-major layout of stride 2^L: FP32 {4 floats, record half, column, row,
+// plane}, FP16 {4 words, column, row, plane}; box = one 36 x 20 halo tile.
+void build_tensor_maps(tg_svgf* s)
+{
+    s->tma = false;
+    if (s->p.mode != TG_SVGF_MODE_FULL || (s->flags & TG_SVGF_FLAG_NO_TMA)) return;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return;
+    const bool f16 = s->p.storage == TG_SVGF_STORAGE_FP16;
+    for (int lv = 0; lv < s->p.levels; ++lv) {
+        const ResLayout L = res_layout(int(s->w), int(s->h), lv);
+        void* base = (lv & 1) ? s->colB : s->colA;
+        const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
+        CUresult r;
+        if (f16) {
+            const cuuint64_t dim[4] = {4, cuuint64_t(L.pw), cuuint64_t(L.ph), planes};
+            const cuuint64_t str[3] = {16, 16ull * L.pw, 16ull * L.pw * L.ph};
+            const cuuint32_t box[4] = {4, LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1};
+            const cuuint32_t es[4] = {1, 1, 1, 1};
+            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, base, dim, str, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        } else {
+            const cuuint64_t dim[5] = {4, 2, cuuint64_t(L.pw), cuuint64_t(L.ph), planes};
+            const cuuint64_t str[4] = {16, 32, 32ull * L.pw, 32ull * L.pw * L.ph};
+            const cuuint32_t box[5] = {4, 1, LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1};
+            const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, base, dim, str, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        }
+        if (r != CUDA_SUCCESS) return;
+    }
+    s->tma = true;
 }
 
 void free_buffers(tg_svgf* s)
@@ -297,6 +366,7 @@ int alloc_buffers(tg_svgf* s)
         return fail(TG_ERR_OOM, "cudaMalloc of %zu scratch bytes failed", s->scratch_bytes);
     }
     carve(s);
+    build_tensor_maps(s);
     if (cudaMemset(s->state, 0, s->state_bytes) != cudaSuccess || cudaMemset(s->scratch, 0, s->scratch_bytes) != cudaSuccess ||
         cudaDeviceSynchronize() != cudaSuccess) {
         free_buffers(s);
@@ -326,9 +396,6 @@ int check_inputs(const tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outpu
 } // namespace
 
 namespace tg {
-
-// Output rows per thread of the tiled a-trous kernels.
-constexpr int kLevelR = 2;
 
 static cudaEvent_t prof_event(tg_svgf* s)
 {
@@ -428,6 +495,7 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.mom_cur = s->mom[cur];
         a.tc = s->tc;
         a.grad = s->grad;
+        a.err = s->d_err;
         a.alpha = s->p.alpha;
         a.alpha_m = s->p.moments_alpha;
         a.sigma_l = s->p.sigma_l;
@@ -449,8 +517,8 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             else
                 k_full_temporal<ST_FP32><<<grd, blk, 0, stream>>>(a);
         });
-        // variance: tc + moments in, col out
-        launch(s, stream, F_FULL_VARIANCE, npx * (2 * c4 + mm), [&] {
+        // variance: tc + moments + guide in, level-0 records out
+        launch(s, stream, F_FULL_VARIANCE, npx * (c4 + mm + gb + (f16 ? 16 : 32)), [&] {
             if (f16)
                 k_full_variance<ST_FP16><<<grd, blk, 0, stream>>>(a);
             else
@@ -466,15 +534,24 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             a.last = lv == s->p.levels - 1;
             a.lin = res_layout(a.w, a.h, lv);
             a.lout = res_layout(a.w, a.h, lv + 1);
-            // level: col + guide + depth gradient in, col (or output) out; level 0 also tc in, history out
-            const double lb = c4 + gb + 8 + (a.last ? ob : c4) + (lv == 0 ? 2 * c4 : 0);
+            // level: records (colour, variance, guide) + depth gradient in, records (or the output) out;
+            // level 0 also reads the temporal colour's length and writes the history
+            const double rb = f16 ? 16 : 32;
+            const double lb = rb + 8 + (a.last ? ob : rb) + (lv == 0 ? 2 * c4 : 0);
             const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
             const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
             launch(s, stream, F_FULL_LEVEL, npx * lb, [&] {
-                if (f16)
+                if (s->tma) {
+                    const LevelArgs la = level_args_of(a);
+                    if (f16)
+                        k_full_level_tma<ST_FP16, kLevelR><<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv]);
+                    else
+                        k_full_level_tma<ST_FP32, kLevelR><<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv]);
+                } else if (f16) {
                     k_full_level_tiled<ST_FP16, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
-                else
+                } else {
                     k_full_level_tiled<ST_FP32, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
+                }
             });
             void* t = src;
             src = oth;
@@ -571,6 +648,7 @@ int tg_svgf_create(const tg_svgf_desc* desc, tg_svgf** out)
     s->w = desc->width;
     s->h = desc->height;
     s->p = desc->params;
+    s->flags = desc->flags;
     st = alloc_buffers(s);
     if (st) {
         delete s;
@@ -668,6 +746,15 @@ int tg_svgf_denoise_host(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_out
     return TG_OK;
 }
 
+static int read_err(const tg_svgf* s, int* v)
+{
+    *v = 0;
+    if (!s->d_err) return TG_OK;
+    if (cudaMemcpy(v, s->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(TG_ERR_CUDA, "error word read failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return TG_OK;
+}
+
 int tg_svgf_synchronize(tg_svgf* s)
 {
     if (!s) return fail(TG_ERR_INVALID, "null handle");
@@ -675,6 +762,10 @@ int tg_svgf_synchronize(tg_svgf* s)
     for (auto& sg : s->stg)
         if (sg.used && cudaEventSynchronize(sg.ev_done) != cudaSuccess)
             return fail(TG_ERR_CUDA, "synchronize failed: %s", cudaGetErrorString(cudaGetLastError()));
+    int e = 0;
+    int st = read_err(s, &e);
+    if (st) return st;
+    if (e) return fail(TG_ERR_TIMEOUT, "a bounded device-side wait gave up; results since are invalid");
     return TG_OK;
 }
 
@@ -714,7 +805,12 @@ int tg_svgf_get_info(const tg_svgf* s, tg_svgf_info* info)
     info->scratch_bytes = s->scratch_bytes;
     info->staging_bytes = s->stg[0].bytes + s->stg[1].bytes;
     info->kernels_per_frame = uint32_t(s->p.levels + (s->p.mode == TG_SVGF_MODE_FULL ? 2 : 1));
-    return TG_OK;
+    info->tma = s->tma ? 1u : 0u;
+    int e = 0;
+    DeviceGuard g(s->device);
+    const int st = read_err(s, &e);
+    info->device_errors = uint32_t(e);
+    return st;
 }
 
 int tg_svgf_profile_enable(tg_svgf* s, int enable)

@@ -388,7 +388,7 @@ int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
     for (int j = 0; j < b->n; ++j) {
         const size_t np = size_t(b->w[j]) * b->h[j];
         const size_t sb = state_bytes_of(b->p, b->w[j], b->h[j]);
-        const size_t cb = al256(np * c4) + al256(np * sizeof(float2)) + 2 * al256(col_pixels_of(b->p, b->w[j], b->h[j]) * c4);
+        const size_t cb = al256(np * c4) + al256(np * sizeof(float2)) + 2 * al256(col_pixels_of(b->p, b->w[j], b->h[j]) * rec_bytes_of(b->p));
         b->state_bytes += sb;
         b->scratch_bytes += cb;
         off[j + 1] = off[j] + sb + cb;
@@ -422,7 +422,7 @@ int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
         p += al256(np * c4);
         s.grad = reinterpret_cast<float2*>(p);
         p += al256(np * sizeof(float2));
-        const size_t colb = al256(col_pixels_of(b->p, b->w[j], b->h[j]) * c4);
+        const size_t colb = al256(col_pixels_of(b->p, b->w[j], b->h[j]) * rec_bytes_of(b->p));
         s.colA = p;
         p += colb;
         s.colB = p;

@@ -271,6 +271,25 @@ template <> struct Stor<ST_FP32> {
     __device__ static float2 ldm(const mom_t* p, size_t i) { return __ldg(p + i); }
     __device__ static void stm(mom_t* p, size_t i, float2 v) { p[i] = v; }
     __device__ static float qin(float v) { return v; }
+    // a-trous scratch record (32 B): float4 (r, g, b, var) then the guide float4 (n, z)
+    typedef float4 rec_t;
+    typedef float4 graw_t;
+    static constexpr int kRecBytes = 32;
+    __device__ static graw_t ld_graw(const guide_t* p, size_t i) { return __ldg(p + i); }
+    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g)
+    {
+        c = __ldg(p + 2 * i);
+        g = __ldg(p + 2 * i + 1);
+    }
+    __device__ static float ld_rec_var(const rec_t* p, size_t i)
+    {
+        return __ldg(reinterpret_cast<const float*>(p + 2 * i) + 3);
+    }
+    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g)
+    {
+        p[2 * i] = c;
+        p[2 * i + 1] = g;
+    }
 };
 
 template <> struct Stor<ST_FP16> {
@@ -310,6 +329,27 @@ template <> struct Stor<ST_FP16> {
     __device__ static float2 ldm(const mom_t* p, size_t i) { return unpack_h2(__ldg(p + i)); }
     __device__ static void stm(mom_t* p, size_t i, float2 v) { p[i] = pack_h2(sat16(v.x), sat16(v.y)); }
     __device__ static float qin(float v) { return q16(v); }
+    // a-trous scratch record (16 B): half (r, g), half (b, var), octahedral code, z bits
+    typedef uint4 rec_t;
+    typedef uint2 graw_t;
+    static constexpr int kRecBytes = 16;
+    __device__ static graw_t ld_graw(const guide_t* p, size_t i) { return __ldg(p + i); }
+    __device__ static void decode_rec(uint4 u, float4& c, float4& g)
+    {
+        const float2 a = unpack_h2(u.x), b = unpack_h2(u.y);
+        c = make_float4(a.x, a.y, b.x, b.y);
+        const float3 n = oct16_decode_fast(u.z);
+        g = make_float4(n.x, n.y, n.z, __uint_as_float(u.w));
+    }
+    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g) { decode_rec(__ldg(p + i), c, g); }
+    __device__ static float ld_rec_var(const rec_t* p, size_t i)
+    {
+        return unpack_h2(__ldg(reinterpret_cast<const uint32_t*>(p + i) + 1)).y;
+    }
+    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g)
+    {
+        p[i] = make_uint4(pack_h2(c.x, c.y), pack_h2(c.z, sat16(c.w)), g.x, g.y);
+    }
 };
 
 // One-sided depth difference with the smaller magnitude (0 for a 1-pixel axis).

@@ -27,5 +27,7 @@ size_t state_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 // Pixels of one a-trous scratch image in the largest residue-major layout used.
 size_t col_pixels_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
+// Bytes of one a-trous scratch record (FULL: colour, variance and guide).
+size_t rec_bytes_of(const tg_svgf_params& p);
 
 } // namespace tg

@@ -97,6 +97,7 @@ struct FullArgs {
     const void* col_src;
     void* col_dst;
     float2* grad;           // per-pixel depth gradient (written by the temporal kernel)
+    int* err;               // device error word (bounded waits that gave up); may be null
     ResLayout lin, lout;    // scratch layouts of col_src and col_dst
     float alpha, alpha_m, sigma_l, sigma_n, sigma_z;
     int sq_n; // squarings for sigma_n = 2^sq_n, -1 otherwise
@@ -271,7 +272,8 @@ template <int ST> __device__ __forceinline__ void full_variance_px(const FullArg
             var = fmaxf(0.0f, s2 / s0 - m1 * m1);
         }
     }
-    S::st4_sat_w(static_cast<C4*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var));
+    // level-0 input record: colour + variance, and the pixel's guide for the edge stops
+    S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var), S::ld_graw(gc, i));
 }
 
 template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY, 4) k_full_temporal(FullArgs a)

@@ -26,6 +26,8 @@
 // record is read from shared memory once for up to R outputs.
 #pragma once
 
+#include <cuda.h>
+
 #include "svgf_device.cuh"
 
 namespace tg {
@@ -55,10 +57,13 @@ template <int R> struct LevelTile {
     static constexpr int N = SW * SH;
 };
 
-template <int R> struct LevelSmem {
-    float4 A[LevelTile<R>::N];
-    float4 N[LevelTile<R>::N];
-    float V[LevelTile<R>::N];
+// Staged tile of one level: X0 = (r, g, b, variance), X1 = (unit normal, depth),
+// XL = luminance.  X0 and X1 are 128-byte aligned so that a TMA box can land
+// in them directly (N * 16 bytes is a multiple of 128 for both tile shapes).
+template <int R> struct __align__(128) LevelSmem {
+    float4 X0[LevelTile<R>::N];
+    float4 X1[LevelTile<R>::N];
+    float XL[LevelTile<R>::N];
 };
 
 // Maps tile `bid` to (residue a, b) and its tile origin in sub-lattice units.
@@ -96,34 +101,28 @@ __host__ __device__ inline LevelArgs level_args_of(const FullArgs& a)
     return l;
 }
 
-// One tile of one level.  The caller synchronises the CTA before reusing `sm`.
+// Per-centre values read from global memory before the tile is staged, so
+// that their latency overlaps the staging: the depth gradient, the 3x3
+// variance neighbourhood (contiguous in the residue-major layout: the index of
+// (qx, qy) separates into a column and a row term) and, for FP16 storage, the
+// centre's raw guide that the output record carries on.
+template <int ST, int R> struct CentrePre {
+    float vn9[R][9];
+    float2 gr[R];
+    typename Stor<ST>::graw_t graw[R];
+    bool valid[R];
+    float kx_sum;
+};
+
 template <int ST, int R>
-__device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
-                                                LevelSmem<R>& sm)
+__device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArgs& lv, int s, int ra, int rb, int i0,
+                                               int j0, CentrePre<ST, R>& pre)
 {
     typedef Stor<ST> S;
-    typedef typename S::guide_t G;
-    typedef typename S::c4_t C4;
-    typedef LevelTile<R> T;
-    float4* sA = sm.A;
-    float4* sN = sm.N;
-    float* sV = sm.V;
-
-    int ra, rb, i0, j0;
-    level_block(g, bid, T::TX, T::TY, ra, rb, i0, j0);
-    const int s = g.s, lg = lv.lin.lg, m = s - 1;
-    const int pw = lv.lin.pw;
-    const int P = lv.lin.pw * lv.lin.ph;  // elements per residue plane (< 2^31)
-    const C4* src = static_cast<const C4*>(lv.col_src);
-    const G* gc = static_cast<const G*>(a.guide_cur);
-    const int ci = threadIdx.x;         // tile column of this thread's outputs
-    const int cj0 = threadIdx.y * R;    // first tile row of this thread's outputs
-    const int cx = ra + s * (i0 + ci);
-
-    // ---- per-centre global reads first, so that their latency overlaps the
-    // staging below: the depth gradient and the 3x3 variance neighbourhood.
-    // In the residue-major layout the index of (qx, qy) separates into a
-    // column term and a row term, and a warp's 32 reads are contiguous.
+    typedef typename S::rec_t RT;
+    const RT* src = static_cast<const RT*>(lv.col_src);
+    const int lg = lv.lin.lg, m = s - 1, pw = lv.lin.pw, P = lv.lin.pw * lv.lin.ph;
+    const int cx = ra + s * (i0 + int(threadIdx.x));
     int cxo[3];
     bool cxv[3];
 #pragma unroll
@@ -132,46 +131,49 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
         cxv[e] = unsigned(qx) < unsigned(a.w);
         cxo[e] = (qx & m) * P + (qx >> lg);
     }
-    const float kx_sum = (cxv[0] ? 0.25f : 0.f) + (cxv[1] ? 0.5f : 0.f) + (cxv[2] ? 0.25f : 0.f);
-    float vn9[R][9];
-    float2 gr[R];
-    bool valid[R];
+    pre.kx_sum = (cxv[0] ? 0.25f : 0.f) + (cxv[1] ? 0.5f : 0.f) + (cxv[2] ? 0.25f : 0.f);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        const int y = rb + s * (j0 + cj0 + k);
-        valid[k] = cx < a.w && y < a.h;
-        gr[k] = valid[k] ? a.grad[y * a.w + cx] : make_float2(0.f, 0.f);
+        const int y = rb + s * (j0 + int(threadIdx.y) * R + k);
+        pre.valid[k] = cx < a.w && y < a.h;
+        pre.gr[k] = pre.valid[k] ? a.grad[y * a.w + cx] : make_float2(0.f, 0.f);
+        if (ST == ST_FP16)
+            pre.graw[k] = pre.valid[k] ? S::ld_graw(static_cast<const typename S::guide_t*>(a.guide_cur), y * a.w + cx)
+                                       : typename S::graw_t{};
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const int qy = y + f - 1;
-            const bool oy = valid[k] && unsigned(qy) < unsigned(a.h);
+            const bool oy = pre.valid[k] && unsigned(qy) < unsigned(a.h);
             const int ro = ((qy & m) << lg) * P + (qy >> lg) * pw;
 #pragma unroll
-            for (int e = 0; e < 3; ++e) vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::ld4_w(src, ro + cxo[e]) : 0.f;
+            for (int e = 0; e < 3; ++e) pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::ld_rec_var(src, ro + cxo[e]) : 0.f;
         }
     }
+}
 
-    // ---- stage the tile: (TX+4) x (TY+4) sub-lattice pixels, zero outside.
-    const int plane = ((rb << lg) + ra) * P;
-    for (int k = threadIdx.y * kLvTX + threadIdx.x; k < T::N; k += kLvTX * kLvRows) {
-        const int sj = k / T::SW, si = k - sj * T::SW;
-        const int j = j0 + sj - 2, i = i0 + si - 2;
-        const int y = rb + s * j, x = ra + s * i;
-        float4 va = make_float4(0.f, 0.f, 0.f, 0.f), vn = make_float4(0.f, 0.f, 0.f, 0.f);
-        float vv = 0.f;
-        if (j >= 0 && i >= 0 && y < a.h && x < a.w) {
-            const float4 c = S::ld4(src, plane + j * pw + i);
-            va = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
-            vv = c.w;
-            vn = S::ld_guide_w(gc, y * a.w + x);
-        }
-        sA[k] = va;
-        sN[k] = vn;
-        sV[k] = vv;
-    }
-    __syncthreads();
+// Whether staged tile cell k (sub-lattice coordinates relative to the tile) is
+// a pixel of the image; cells outside are zero records with weight 0.
+template <int R>
+__device__ __forceinline__ bool staged_inside(const FullArgs& a, int s, int ra, int rb, int i0, int j0, int k)
+{
+    typedef LevelTile<R> T;
+    const int sj = k / T::SW, si = k - sj * T::SW;
+    const int j = j0 + sj - 2, i = i0 + si - 2;
+    return j >= 0 && i >= 0 && rb + s * j < a.h && ra + s * i < a.w;
+}
 
-    // ---- per-centre set-up.  Exponent factors are pre-scaled by log2(e).
+// Everything after staging: per-centre set-up, the taps, the output records.
+template <int ST, int R>
+__device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra,
+                                              int rb, int i0, int j0, const CentrePre<ST, R>& pre,
+                                              const LevelSmem<R>& sm)
+{
+    typedef Stor<ST> S;
+    typedef typename S::c4_t C4;
+    typedef LevelTile<R> T;
+    const int s = g.s;
+    const int ci = threadIdx.x, cj0 = threadIdx.y * R;
+    const int cx = ra + s * (i0 + ci);
     float lp[R], kl[R], zp[R], nx[R], ny[R], nz[R], kz[R][13];
     float ar[R], ag[R], ab[R], aw[R], av[R];
     const float zs = a.sigma_z * float(s) * (1.0f / kLog2e);
@@ -179,8 +181,8 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int c = (cj0 + k + 2) * T::SW + ci + 2;
-        const float4 A = sA[c], N = sN[c];
-        lp[k] = A.w;
+        const float4 N = sm.X1[c];
+        lp[k] = sm.XL[c];
         zp[k] = N.w;
         nx[k] = N.x;
         ny[k] = N.y;
@@ -192,10 +194,11 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
                              (unsigned(y + 1) < unsigned(a.h) ? 0.25f : 0.f);
         float sv = 0.f;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) sv = fmaf((q / 3 == 1 ? 0.5f : 0.25f) * (q % 3 == 1 ? 0.5f : 0.25f), vn9[k][q], sv);
-        const float gv = sv * rcp_approx(ky_sum * kx_sum);
+        for (int q = 0; q < 9; ++q)
+            sv = fmaf((q / 3 == 1 ? 0.5f : 0.25f) * (q % 3 == 1 ? 0.5f : 0.25f), pre.vn9[k][q], sv);
+        const float gv = sv * rcp_approx(ky_sum * pre.kx_sum);
         kl[k] = kLog2e * rcp_approx(a.sigma_l * sqrt_approx(fmaxf(gv, 0.f)) + kEpsL);
-        const float A_ = zs * gr[k].x, B_ = zs * gr[k].y;
+        const float A_ = zs * pre.gr[k].x, B_ = zs * pre.gr[k].y;
         // kz for the 13 offsets (dx, dy) with dy > 0 or (dy == 0 and dx >= 0);
         // the other 12 offsets are their negations and share the value.
 #pragma unroll
@@ -206,12 +209,12 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
         }
     }
 
-    // ---- taps: rows r = 0 .. R+3 of this thread's strip, 5 columns each.
-    // A warp (one strip row of 32 columns) whose outputs all lie outside the
-    // sub-lattice skips the taps.
+    // Taps: rows r = 0 .. R+3 of this thread's strip, 5 columns each.  A warp
+    // (one strip row of 32 columns) whose outputs all lie outside the
+    // sub-lattice skips them.
     bool any_valid = false;
 #pragma unroll
-    for (int k = 0; k < R; ++k) any_valid |= valid[k];
+    for (int k = 0; k < R; ++k) any_valid |= pre.valid[k];
     const float sn = a.sigma_n;
     if (__any_sync(0xffffffffu, any_valid)) {
 #pragma unroll
@@ -219,8 +222,8 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
 #pragma unroll
             for (int dx = -2; dx <= 2; ++dx) {
                 const int q = (cj0 + r) * T::SW + ci + 2 + dx;
-                const float4 A = sA[q], N = sN[q];
-                const float V = sV[q];
+                const float4 A = sm.X0[q], N = sm.X1[q];
+                const float L = sm.XL[q];
 #pragma unroll
                 for (int k = 0; k < R; ++k) {
                     const int dy = r - 2 - k;
@@ -230,48 +233,201 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
                     const int qi = ddy == 0 ? ddx : 3 + (ddy - 1) * 5 + (ddx + 2);
                     const float d = fmaf(nz[k], N.z, fmaf(ny[k], N.y, nx[k] * N.x));
                     float t = fmaf(-fabsf(zp[k] - N.w), kz[k][qi], log2_b3(dx + 2) + log2_b3(dy + 2));
-                    t = fmaf(-fabsf(lp[k] - A.w), kl[k], t);
+                    t = fmaf(-fabsf(lp[k] - L), kl[k], t);
                     t = fmaf(sn, lg2_approx(fmaxf(d, 0.f)), t);
                     const float w = ex2_approx(t);
                     ar[k] = fmaf(w, A.x, ar[k]);
                     ag[k] = fmaf(w, A.y, ag[k]);
                     ab[k] = fmaf(w, A.z, ab[k]);
                     aw[k] += w;
-                    av[k] = fmaf(w * w, V, av[k]);
+                    av[k] = fmaf(w * w, A.w, av[k]);
                 }
             }
         }
     }
 
-    // ---- outputs.
+    // Outputs: the next level's record (colour, variance, the centre's guide),
+    // the colour history at level 0, the caller's image at the last level.
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!valid[k]) continue;
+        if (!pre.valid[k]) continue;
         const int y = rb + s * (j0 + cj0 + k);
         const int i = y * a.w + cx;
+        const int c = (cj0 + k + 2) * T::SW + ci + 2;
         float4 o;
         if (aw[k] > 0.f) {
             const float inv = rcp_approx(aw[k]);
             o = make_float4(ar[k] * inv, ag[k] * inv, ab[k] * inv, av[k] * (inv * inv));
         } else {
-            const int c = (cj0 + k + 2) * T::SW + ci + 2;
-            o = make_float4(sA[c].x, sA[c].y, sA[c].z, sV[c]);
+            o = sm.X0[c];
         }
         if (lv.level == 0) {
             const float len = S::ld4_w(static_cast<const C4*>(a.tc), i);
             S::st4(static_cast<C4*>(a.hist_cur), i, make_float4(o.x, o.y, o.z, len));
         }
-        if (lv.last)
+        if (lv.last) {
             st_rgba(a.out, cx, y, make_float4(S::qin(o.x), S::qin(o.y), S::qin(o.z), 1.0f));
-        else
-            S::st4_sat_w(static_cast<C4*>(lv.col_dst), res_idx(lv.lout, cx, y), o);
+        } else {
+            typename S::graw_t graw;
+            if constexpr (ST == ST_FP16)
+                graw = pre.graw[k];
+            else
+                graw = sm.X1[c];
+            S::st_rec(static_cast<typename S::rec_t*>(lv.col_dst), res_idx(lv.lout, cx, y), o, graw);
+        }
     }
+}
+
+// One tile of one level, staged with plain coalesced loads (the residue-major
+// records of a tile row are contiguous).  The caller synchronises the CTA
+// before reusing `sm`.
+template <int ST, int R>
+__device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
+                                                LevelSmem<R>& sm)
+{
+    typedef Stor<ST> S;
+    typedef typename S::rec_t RT;
+    typedef LevelTile<R> T;
+    int ra, rb, i0, j0;
+    level_block(g, bid, T::TX, T::TY, ra, rb, i0, j0);
+    const int s = g.s;
+    CentrePre<ST, R> pre;
+    level_prefetch<ST, R>(a, lv, s, ra, rb, i0, j0, pre);
+    const RT* src = static_cast<const RT*>(lv.col_src);
+    const int pw = lv.lin.pw, P = lv.lin.pw * lv.lin.ph;
+    const int plane = ((rb << lv.lin.lg) + ra) * P;
+    for (int k = threadIdx.y * kLvTX + threadIdx.x; k < T::N; k += kLvTX * kLvRows) {
+        float4 c = make_float4(0.f, 0.f, 0.f, 0.f), n = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
+            const int sj = k / T::SW, si = k - sj * T::SW;
+            S::ld_rec(src, plane + (j0 + sj - 2) * pw + (i0 + si - 2), c, n);
+        }
+        sm.X0[k] = c;
+        sm.X1[k] = n;
+        sm.XL[k] = lum(c.x, c.y, c.z);
+    }
+    __syncthreads();
+    level_compute<ST, R>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
 template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
     __shared__ LevelSmem<R> sm;
     full_level_tile<ST, R>(a, level_args_of(a), g, blockIdx.x, sm);
+}
+
+// ------------------------------------------------------- TMA-staged level ----
+//
+// The same level with the halo tile staged by the tensor-memory accelerator:
+// one elected thread issues cp.async.bulk.tensor for the tile's box of
+// residue-major records (5-D map {4 floats, record half, column, row, plane}
+// for FP32, so that the box of each record half lands as one dense float4
+// array; 4-D map {4 words, column, row, plane} for FP16), completion is
+// tracked by an mbarrier transaction count, and cells outside the plane array
+// arrive zero-filled.  The wait is bounded: a box that has not landed after
+// about a second sets a->err and the CTA returns.
+
+constexpr long long kTmaWaitCycles = 2000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase)
+{
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(phase)
+                     : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > kTmaWaitCycles) return false;
+    }
+}
+
+template <int ST, int R> struct TmaRaw {
+    uint4 v[1];
+};
+template <int R> struct TmaRaw<ST_FP16, R> {
+    uint4 v[LevelTile<R>::N];
+};
+
+template <int ST, int R>
+__global__ void __launch_bounds__(kLvTX* kLvRows, 3)
+    k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm)
+{
+    typedef LevelTile<R> T;
+    __shared__ LevelSmem<R> sm;
+    __shared__ __align__(128) TmaRaw<ST, R> raw;
+    __shared__ __align__(8) uint64_t bar;
+    int ra, rb, i0, j0;
+    level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
+    const int s = g.s;
+    const int tid = threadIdx.y * kLvTX + threadIdx.x;
+    const uint32_t ubar = smem_u32(&bar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const int plane = (rb << lv.lin.lg) + ra;
+    if (tid == 0) {
+        const uint64_t map = reinterpret_cast<uint64_t>(&tm);
+        if constexpr (ST == ST_FP32) {
+            const uint32_t bytes = 2u * T::N * 16u;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const uint32_t dst = smem_u32(half == 0 ? sm.X0 : sm.X1);
+                asm volatile(
+                    "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+                    "%6}], [%7];" ::"r"(dst),
+                    "l"(map), "r"(0), "r"(half), "r"(i0 - 2), "r"(j0 - 2), "r"(plane), "r"(ubar)
+                    : "memory");
+            }
+        } else {
+            const uint32_t bytes = T::N * 16u;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+                "[%6];" ::"r"(smem_u32(raw.v)),
+                "l"(map), "r"(0), "r"(i0 - 2), "r"(j0 - 2), "r"(plane), "r"(ubar)
+                : "memory");
+        }
+    }
+    CentrePre<ST, R> pre;
+    level_prefetch<ST, R>(a, lv, s, ra, rb, i0, j0, pre);
+    const bool landed = mbar_wait_bounded(ubar, 0);
+    if (__syncthreads_or(!landed)) {
+        if (tid == 0) {
+            if (a.err) atomicExch(a.err, 1);
+            mbar_wait_bounded(ubar, 0);  // give the copy a second bounded chance to retire
+        }
+        return;
+    }
+    // Zero the cells outside the image, compute luminance (and decode FP16 records).
+    for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+        const bool in = staged_inside<R>(a, s, ra, rb, i0, j0, k);
+        float4 c, n;
+        if constexpr (ST == ST_FP16) {
+            Stor<ST_FP16>::decode_rec(raw.v[k], c, n);
+        } else {
+            c = sm.X0[k];
+            n = sm.X1[k];
+        }
+        if (!in) {
+            c = make_float4(0.f, 0.f, 0.f, 0.f);
+            n = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        if (ST == ST_FP16 || !in) {
+            sm.X0[k] = c;
+            sm.X1[k] = n;
+        }
+        sm.XL[k] = lum(c.x, c.y, c.z);
+    }
+    __syncthreads();
+    level_compute<ST, R>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
 // ------------------------------------------------------------- REF-EXACT ----

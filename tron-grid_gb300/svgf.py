@@ -66,13 +66,13 @@ class Denoiser:
     """One SVGF stream (a handle of the C ABI)."""
 
     def __init__(self, width: int, height: int, mode: int = L.MODE_FULL, storage: int = L.STORAGE_FP32,
-                 device: int | None = None, **params):
+                 device: int | None = None, flags: int = 0, **params):
         self.lib = L.load()
         self.params = L.default_params(mode, storage, **params)
         if device is None:
             device = torch.cuda.current_device()
         self.device = device
-        d = L.Desc(width, height, self.params, device, 0)
+        d = L.Desc(width, height, self.params, device, flags)
         h = C.c_void_p()
         L.check(self.lib.tg_svgf_create(C.byref(d), C.byref(h)))
         self.handle = h
