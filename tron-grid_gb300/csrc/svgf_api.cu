@@ -135,11 +135,24 @@ size_t col_pixels_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
     return n;
 }
 
+size_t col_var_offset_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
+{
+    return align_up(col_pixels_of(p, w, h) * layout_of(p).rec, 256);
+}
+
+size_t col_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
+{
+    const size_t recs = col_var_offset_of(p, w, h);
+    if (p.mode == TG_SVGF_MODE_REF_EXACT) return recs;
+    const size_t vb = p.storage == TG_SVGF_STORAGE_FP16 ? 2 : 4;
+    return recs + align_up(col_pixels_of(p, w, h) * vb, 256);
+}
+
 size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     const size_t n = size_t(w) * h;
     const Layout l = layout_of(p);
-    const size_t col = align_up(col_pixels_of(p, w, h) * l.rec, 256);
+    const size_t col = col_bytes_of(p, w, h);
     if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * col;
     return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256) + 256;
 }
@@ -263,8 +276,8 @@ void carve(tg_svgf* s)
         }
         p = s->scratch;
         s->tc = take(n * l.c4);
-        s->colA = take(col_pixels_of(s->p, s->w, s->h) * l.rec);
-        s->colB = take(col_pixels_of(s->p, s->w, s->h) * l.rec);
+        s->colA = take(col_bytes_of(s->p, s->w, s->h));
+        s->colB = take(col_bytes_of(s->p, s->w, s->h));
         s->grad = static_cast<float2*>(take(n * sizeof(float2)));
         s->d_err = static_cast<int*>(take(sizeof(int)));
     }
@@ -505,6 +518,7 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.max_history = s->p.max_history;
         a.fallback_frames = s->p.fallback_frames;
         a.col_dst = s->colA;
+        a.var_off = col_var_offset_of(s->p, s->w, s->h);
         const double npx = double(s->w) * s->h;
         const double gb = f16 ? 8 : 16, c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
         const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +
@@ -517,8 +531,9 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             else
                 k_full_temporal<ST_FP32><<<grd, blk, 0, stream>>>(a);
         });
-        // variance: tc + moments + guide in, level-0 records out
-        launch(s, stream, F_FULL_VARIANCE, npx * (c4 + mm + gb + (f16 ? 16 : 32)), [&] {
+        const double vb = f16 ? 2 : 4;  // variance plane entry
+        // variance: tc + moments + guide in, level-0 records + variance plane out
+        launch(s, stream, F_FULL_VARIANCE, npx * (c4 + mm + gb + (f16 ? 16 : 32) + vb), [&] {
             if (f16)
                 k_full_variance<ST_FP16><<<grd, blk, 0, stream>>>(a);
             else
@@ -534,10 +549,11 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             a.last = lv == s->p.levels - 1;
             a.lin = res_layout(a.w, a.h, lv);
             a.lout = res_layout(a.w, a.h, lv + 1);
-            // level: records (colour, variance, guide) + depth gradient in, records (or the output) out;
-            // level 0 also reads the temporal colour's length and writes the history
+            // level: records (colour, variance, guide), variance plane and depth gradient in, records and
+            // variance plane (or the output) out; level 0 also reads the temporal colour's length and writes
+            // the history
             const double rb = f16 ? 16 : 32;
-            const double lb = rb + 8 + (a.last ? ob : rb) + (lv == 0 ? 2 * c4 : 0);
+            const double lb = rb + vb + 8 + (a.last ? ob : rb + vb) + (lv == 0 ? 2 * c4 : 0);
             const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
             const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
             launch(s, stream, F_FULL_LEVEL, npx * lb, [&] {

@@ -122,6 +122,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
                 LevelArgs lv;
                 lv.col_src = (L & 1) ? e.colB : e.colA;
                 lv.col_dst = (L & 1) ? e.colA : e.colB;
+                lv.var_off = a.var_off;
                 lv.level = L;
                 lv.last = L == hd.levels - 1;
                 lv.lin = res_layout(a.w, a.h, L);
@@ -187,6 +188,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_ms_level(const char* __re
     LevelArgs lv;
     lv.col_src = (L & 1) ? e.colB : e.colA;
     lv.col_dst = (L & 1) ? e.colA : e.colB;
+    lv.var_off = a.var_off;
     lv.level = L;
     lv.last = L == hd->levels - 1;
     lv.lin = res_layout(a.w, a.h, L);

@@ -281,14 +281,19 @@ template <> struct Stor<ST_FP32> {
         c = __ldg(p + 2 * i);
         g = __ldg(p + 2 * i + 1);
     }
-    __device__ static float ld_rec_var(const rec_t* p, size_t i)
-    {
-        return __ldg(reinterpret_cast<const float*>(p + 2 * i) + 3);
-    }
     __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g)
     {
         p[2 * i] = c;
         p[2 * i + 1] = g;
+    }
+    // variance plane beside the records (`off` bytes after the buffer start), 4 B per record
+    __device__ static float ld_var(const void* buf, size_t off, size_t i)
+    {
+        return __ldg(reinterpret_cast<const float*>(static_cast<const char*>(buf) + off) + i);
+    }
+    __device__ static void st_var(void* buf, size_t off, size_t i, float v)
+    {
+        reinterpret_cast<float*>(static_cast<char*>(buf) + off)[i] = v;
     }
 };
 
@@ -342,13 +347,18 @@ template <> struct Stor<ST_FP16> {
         g = make_float4(n.x, n.y, n.z, __uint_as_float(u.w));
     }
     __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g) { decode_rec(__ldg(p + i), c, g); }
-    __device__ static float ld_rec_var(const rec_t* p, size_t i)
-    {
-        return unpack_h2(__ldg(reinterpret_cast<const uint32_t*>(p + i) + 1)).y;
-    }
     __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g)
     {
         p[i] = make_uint4(pack_h2(c.x, c.y), pack_h2(c.z, sat16(c.w)), g.x, g.y);
+    }
+    // variance plane beside the records, 2 B per record: the same half as the record's
+    __device__ static float ld_var(const void* buf, size_t off, size_t i)
+    {
+        return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(static_cast<const char*>(buf) + off) + i)));
+    }
+    __device__ static void st_var(void* buf, size_t off, size_t i, float v)
+    {
+        reinterpret_cast<unsigned short*>(static_cast<char*>(buf) + off)[i] = __half_as_ushort(__float2half_rn(sat16(v)));
     }
 };
 

@@ -29,5 +29,11 @@ size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 size_t col_pixels_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 // Bytes of one a-trous scratch record (FULL: colour, variance and guide).
 size_t rec_bytes_of(const tg_svgf_params& p);
+// Bytes of one a-trous scratch buffer: the records, then (FULL mode) a compact
+// plane of the records' variances in the same residue-major layout, which the
+// levels read for the 3x3 variance blur.
+size_t col_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
+// Byte offset of that variance plane from the start of the buffer.
+size_t col_var_offset_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 
 } // namespace tg

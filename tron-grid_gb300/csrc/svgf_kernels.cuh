@@ -96,6 +96,7 @@ struct FullArgs {
     void* tc;
     const void* col_src;
     void* col_dst;
+    size_t var_off;         // byte offset of the variance plane in col_src / col_dst
     float2* grad;           // per-pixel depth gradient (written by the temporal kernel)
     int* err;               // device error word (bounded waits that gave up); may be null
     ResLayout lin, lout;    // scratch layouts of col_src and col_dst
@@ -274,6 +275,7 @@ template <int ST> __device__ __forceinline__ void full_variance_px(const FullArg
     }
     // level-0 input record: colour + variance, and the pixel's guide for the edge stops
     S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var), S::ld_graw(gc, i));
+    S::st_var(a.col_dst, a.var_off, i, var);
 }
 
 template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY, 4) k_full_temporal(FullArgs a)

@@ -85,6 +85,7 @@ __device__ __forceinline__ void level_block(const LevelGeom& g, int bid, int TX,
 struct LevelArgs {
     const void* col_src;
     void* col_dst;
+    size_t var_off;  // byte offset of the variance plane in col_src / col_dst
     int level, last;
     ResLayout lin, lout;
 };
@@ -94,6 +95,7 @@ __host__ __device__ inline LevelArgs level_args_of(const FullArgs& a)
     LevelArgs l;
     l.col_src = a.col_src;
     l.col_dst = a.col_dst;
+    l.var_off = a.var_off;
     l.level = a.level;
     l.last = a.last;
     l.lin = a.lin;
@@ -119,8 +121,6 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
                                                int j0, CentrePre<ST, R>& pre)
 {
     typedef Stor<ST> S;
-    typedef typename S::rec_t RT;
-    const RT* src = static_cast<const RT*>(lv.col_src);
     const int lg = lv.lin.lg, m = s - 1, pw = lv.lin.pw, P = lv.lin.pw * lv.lin.ph;
     const int cx = ra + s * (i0 + int(threadIdx.x));
     int cxo[3];
@@ -146,7 +146,7 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
             const bool oy = pre.valid[k] && unsigned(qy) < unsigned(a.h);
             const int ro = ((qy & m) << lg) * P + (qy >> lg) * pw;
 #pragma unroll
-            for (int e = 0; e < 3; ++e) pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::ld_rec_var(src, ro + cxo[e]) : 0.f;
+            for (int e = 0; e < 3; ++e) pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::ld_var(lv.col_src, lv.var_off, ro + cxo[e]) : 0.f;
         }
     }
 }
@@ -273,7 +273,9 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
                 graw = pre.graw[k];
             else
                 graw = sm.X1[c];
-            S::st_rec(static_cast<typename S::rec_t*>(lv.col_dst), res_idx(lv.lout, cx, y), o, graw);
+            const size_t oi = res_idx(lv.lout, cx, y);
+            S::st_rec(static_cast<typename S::rec_t*>(lv.col_dst), oi, o, graw);
+            S::st_var(lv.col_dst, lv.var_off, oi, o.w);
         }
     }
 }
@@ -310,7 +312,7 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
     level_compute<ST, R>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
-template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_full_level_tiled(FullArgs a, LevelGeom g)
+template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, R <= 2 ? 3 : 2) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
     __shared__ LevelSmem<R> sm;
     full_level_tile<ST, R>(a, level_args_of(a), g, blockIdx.x, sm);
@@ -345,21 +347,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase)
     }
 }
 
-template <int ST, int R> struct TmaRaw {
-    uint4 v[1];
-};
-template <int R> struct TmaRaw<ST_FP16, R> {
-    uint4 v[LevelTile<R>::N];
+// CTAs per SM the level kernels are compiled for (register budget).
+template <int R> struct LevelOcc {
+    static constexpr int kCtas = R <= 2 ? 3 : 2;
 };
 
 template <int ST, int R>
-__global__ void __launch_bounds__(kLvTX* kLvRows, 3)
+__global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm)
 {
     typedef LevelTile<R> T;
     __shared__ LevelSmem<R> sm;
-    __shared__ __align__(128) TmaRaw<ST, R> raw;
     __shared__ __align__(8) uint64_t bar;
+    // FP16 records (16 B) land in the X1 array and are decoded in place: each
+    // thread reads raw record k before it writes X0/X1/XL entry k.
+    uint4* raw = reinterpret_cast<uint4*>(sm.X1);
     int ra, rb, i0, j0;
     level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
     const int s = g.s;
@@ -391,7 +393,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3)
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
             asm volatile(
                 "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-                "[%6];" ::"r"(smem_u32(raw.v)),
+                "[%6];" ::"r"(smem_u32(raw)),
                 "l"(map), "r"(0), "r"(i0 - 2), "r"(j0 - 2), "r"(plane), "r"(ubar)
                 : "memory");
         }
@@ -411,7 +413,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3)
         const bool in = staged_inside<R>(a, s, ra, rb, i0, j0, k);
         float4 c, n;
         if constexpr (ST == ST_FP16) {
-            Stor<ST_FP16>::decode_rec(raw.v[k], c, n);
+            Stor<ST_FP16>::decode_rec(raw[k], c, n);
         } else {
             c = sm.X0[k];
             n = sm.X1[k];

@@ -185,7 +185,7 @@ size_t slot_bytes(const tg_svgf_params& p, const Sess& s)
     const bool f16 = p.storage == TG_SVGF_STORAGE_FP16;
     const size_t c4 = f16 ? 8 : 16;
     size_t b = al256(state_bytes_of(p, s.w, s.h));
-    b += al256(np * c4) + al256(np * sizeof(float2)) + 2 * al256(col_pixels_of(p, s.w, s.h) * rec_bytes_of(p));
+    b += al256(np * c4) + al256(np * sizeof(float2)) + 2 * col_bytes_of(p, s.w, s.h);
     for (int k = 0; k < 4; ++k) b += 2 * al256(in_bytes(s, k));
     b += 2 * al256(size_t(fmt_bytes(s.fmt[4])) * np);
     return b;
@@ -210,7 +210,7 @@ void carve(tg_svgf_server* sv, Sess& s)
     p += al256(np * c4);
     s.grad = reinterpret_cast<float2*>(p);
     p += al256(np * sizeof(float2));
-    const size_t colb = al256(col_pixels_of(sv->d.params, s.w, s.h) * rec_bytes_of(sv->d.params));
+    const size_t colb = col_bytes_of(sv->d.params, s.w, s.h);
     s.colA = p;
     p += colb;
     s.colB = p;
@@ -285,6 +285,7 @@ FullArgs args_for(tg_svgf_server* sv, Sess& s)
     a.tc = s.tc;
     a.grad = s.grad;
     a.col_dst = s.colA;
+    a.var_off = col_var_offset_of(sv->d.params, s.w, s.h);
     const tg_svgf_params& p = sv->d.params;
     a.alpha = p.alpha;
     a.alpha_m = p.moments_alpha;
