@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kBlockX* kBlockY) k_ms_pixel(const char* __res
 }
 
 template <int ST, int R>
-__global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_ms_level(const char* __restrict__ table, int cap, int L)
+__global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level(const char* __restrict__ table, int cap, int L)
 {
     __shared__ LevelSmem<R> sm;
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);

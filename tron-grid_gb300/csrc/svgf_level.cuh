@@ -57,6 +57,13 @@ template <int R> struct LevelTile {
     static constexpr int N = SW * SH;
 };
 
+// CTAs per SM the level kernels are compiled for: at R = 2 four CTAs (32
+// warps, 64 registers a thread) hide the tap loop's latencies better than
+// three with 80 registers.
+template <int R> struct LevelOcc {
+    static constexpr int kCtas = R <= 2 ? 4 : 2;
+};
+
 // Staged tile of one level: X0 = (r, g, b, variance), X1 = (unit normal, depth),
 // XL = luminance.  X0 and X1 are 128-byte aligned so that a TMA box can land
 // in them directly (N * 16 bytes is a multiple of 128 for both tile shapes).
@@ -312,7 +319,7 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
     level_compute<ST, R>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
-template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, R <= 2 ? 3 : 2) k_full_level_tiled(FullArgs a, LevelGeom g)
+template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
     __shared__ LevelSmem<R> sm;
     full_level_tile<ST, R>(a, level_args_of(a), g, blockIdx.x, sm);
@@ -346,11 +353,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase)
         if (clock64() - t0 > kTmaWaitCycles) return false;
     }
 }
-
-// CTAs per SM the level kernels are compiled for (register budget).
-template <int R> struct LevelOcc {
-    static constexpr int kCtas = R <= 2 ? 3 : 2;
-};
 
 template <int ST, int R>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
