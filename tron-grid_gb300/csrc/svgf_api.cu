@@ -148,13 +148,19 @@ size_t col_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
     return recs + align_up(col_pixels_of(p, w, h) * vb, 256);
 }
 
+size_t fb_flags_bytes_of(uint32_t w, uint32_t h)
+{
+    return size_t((w + kBlockX - 1) / kBlockX) * ((h + kBlockY - 1) / kBlockY) * sizeof(int);
+}
+
 size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     const size_t n = size_t(w) * h;
     const Layout l = layout_of(p);
     const size_t col = col_bytes_of(p, w, h);
     if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * col;
-    return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256) + 256;
+    return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256) + align_up(fb_flags_bytes_of(w, h), 256) +
+           256;
 }
 
 int validate_params(const tg_svgf_params& p)
@@ -204,6 +210,7 @@ struct tg_svgf {
     void* colA = nullptr;
     void* colB = nullptr;
     float2* grad = nullptr;
+    int* fb_flags = nullptr;
     int* d_err = nullptr;  // device error word of bounded waits
     int flags = 0;
     bool tma = false;                // a-trous tiles staged by TMA
@@ -267,6 +274,7 @@ void carve(tg_svgf* s)
         s->colB = take(col_pixels_of(s->p, s->w, s->h) * l.c4);
         s->guide[0] = s->guide[1] = s->hist[0] = s->hist[1] = s->tc = nullptr;
         s->grad = nullptr;
+        s->fb_flags = nullptr;
         s->d_err = nullptr;
     } else {
         for (int k = 0; k < 2; ++k) {
@@ -279,6 +287,7 @@ void carve(tg_svgf* s)
         s->colA = take(col_bytes_of(s->p, s->w, s->h));
         s->colB = take(col_bytes_of(s->p, s->w, s->h));
         s->grad = static_cast<float2*>(take(n * sizeof(float2)));
+        s->fb_flags = static_cast<int*>(take(fb_flags_bytes_of(s->w, s->h)));
         s->d_err = static_cast<int*>(take(sizeof(int)));
     }
 }
@@ -508,6 +517,7 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.mom_cur = s->mom[cur];
         a.tc = s->tc;
         a.grad = s->grad;
+        a.fb_flags = s->fb_flags;
         a.err = s->d_err;
         a.alpha = s->p.alpha;
         a.alpha_m = s->p.moments_alpha;
@@ -524,16 +534,18 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +
                            fmt_bytes(in->normal.format) + fmt_bytes(in->motion.format);
         const double ob = fmt_bytes(out->denoised.format);
-        // temporal: inputs + previous guide/history/moments, writes guide, tc, moments, depth gradient
-        launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm) + 8), [&] {
+        const double vb = f16 ? 2 : 4;    // variance plane entry
+        const double rb = f16 ? 16 : 32;  // a-trous record
+        // temporal: inputs + previous guide/history/moments, writes guide, tc, moments, depth gradient and
+        // the level-0 record + variance plane entry (every pixel with a history of fallback_frames or more)
+        launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm) + 8 + rb + vb), [&] {
             if (f16)
                 k_full_temporal<ST_FP16><<<grd, blk, 0, stream>>>(a);
             else
                 k_full_temporal<ST_FP32><<<grd, blk, 0, stream>>>(a);
         });
-        const double vb = f16 ? 2 : 4;  // variance plane entry
-        // variance: tc + moments + guide in, level-0 records + variance plane out
-        launch(s, stream, F_FULL_VARIANCE, npx * (c4 + mm + gb + (f16 ? 16 : 32) + vb), [&] {
+        // variance: the block flags; the flagged blocks' short-history pixels (data-dependent, not counted)
+        launch(s, stream, F_FULL_VARIANCE, double(fb_flags_bytes_of(s->w, s->h)), [&] {
             if (f16)
                 k_full_variance<ST_FP16><<<grd, blk, 0, stream>>>(a);
             else
@@ -552,7 +564,6 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             // level: records (colour, variance, guide), variance plane and depth gradient in, records and
             // variance plane (or the output) out; level 0 also reads the temporal colour's length and writes
             // the history
-            const double rb = f16 ? 16 : 32;
             const double lb = rb + vb + 8 + (a.last ? ob : rb + vb) + (lv == 0 ? 2 * c4 : 0);
             const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
             const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);

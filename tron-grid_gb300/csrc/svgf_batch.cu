@@ -36,6 +36,7 @@ struct tg_svgf_batch {
         void* mom[2];
         void* tc;
         float2* grad;
+        int* fb_flags;
         void* colA;
         void* colB;
         char* state;
@@ -276,6 +277,7 @@ void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const 
         a.mom_cur = s.mom[cur];
         a.tc = s.tc;
         a.grad = s.grad;
+        a.fb_flags = s.fb_flags;
         a.col_dst = s.colA;
         a.var_off = col_var_offset_of(b->p, W, b->h[ids[j]]);
         a.alpha = b->p.alpha;
@@ -389,7 +391,8 @@ int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
     for (int j = 0; j < b->n; ++j) {
         const size_t np = size_t(b->w[j]) * b->h[j];
         const size_t sb = state_bytes_of(b->p, b->w[j], b->h[j]);
-        const size_t cb = al256(np * c4) + al256(np * sizeof(float2)) + 2 * col_bytes_of(b->p, b->w[j], b->h[j]);
+        const size_t cb = al256(np * c4) + al256(np * sizeof(float2)) + al256(fb_flags_bytes_of(b->w[j], b->h[j])) +
+                          2 * col_bytes_of(b->p, b->w[j], b->h[j]);
         b->state_bytes += sb;
         b->scratch_bytes += cb;
         off[j + 1] = off[j] + sb + cb;
@@ -423,6 +426,8 @@ int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
         p += al256(np * c4);
         s.grad = reinterpret_cast<float2*>(p);
         p += al256(np * sizeof(float2));
+        s.fb_flags = reinterpret_cast<int*>(p);
+        p += al256(fb_flags_bytes_of(b->w[j], b->h[j]));
         const size_t colb = col_bytes_of(b->p, b->w[j], b->h[j]);
         s.colA = p;
         p += colb;

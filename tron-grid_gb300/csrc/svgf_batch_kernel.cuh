@@ -83,12 +83,15 @@ __device__ __forceinline__ bool grid_barrier(BarrierState* b, unsigned nblocks, 
     return ok != 0;
 }
 
+// The persistent kernel runs the pixel stages on its level-shaped CTAs.
+static_assert(kLvTX == kBlockX && kLvRows == kBlockY, "pixel and level CTAs must have the same shape");
+
 template <int ST, int R>
 __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __restrict__ table, int cap,
                                                                    BarrierState* bar, unsigned expect_blocks,
                                                                    long long spin_cycles)
 {
-    __shared__ LevelSmem<R> sm;
+    __shared__ LevelSmem<R, ST> sm;
     const BatchHeader hd = *reinterpret_cast<const BatchHeader*>(table);
     const int* prefix = reinterpret_cast<const int*>(table + table_prefix_offset());
     const BatchEntry* ent = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap));
@@ -111,12 +114,10 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
                 const int tx = (a.w + kBlockX - 1) / kBlockX;
                 const int x = (local % tx) * kBlockX + threadIdx.x;
                 const int y = (local / tx) * kBlockY + threadIdx.y;
-                if (x < a.w && y < a.h) {
-                    if (stage == 0)
-                        full_temporal_px<ST>(a, x, y);
-                    else
-                        full_variance_px<ST>(a, x, y);
-                }
+                if (stage == 0)
+                    full_temporal_block<ST>(a, local, x, y);
+                else
+                    full_variance_block<ST>(a, local, x, y);
             } else {
                 const int L = stage - 2;
                 LevelArgs lv;
@@ -167,17 +168,16 @@ __global__ void __launch_bounds__(kBlockX* kBlockY) k_ms_pixel(const char* __res
     const int tx = (a.w + kBlockX - 1) / kBlockX;
     const int x = (local % tx) * kBlockX + threadIdx.x;
     const int y = (local / tx) * kBlockY + threadIdx.y;
-    if (x >= a.w || y >= a.h) return;
     if (STAGE == 0)
-        full_temporal_px<ST>(a, x, y);
+        full_temporal_block<ST>(a, local, x, y);
     else
-        full_variance_px<ST>(a, x, y);
+        full_variance_block<ST>(a, local, x, y);
 }
 
 template <int ST, int R>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level(const char* __restrict__ table, int cap, int L)
 {
-    __shared__ LevelSmem<R> sm;
+    __shared__ LevelSmem<R, ST> sm;
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
     const int item = blockIdx.x;

@@ -270,6 +270,9 @@ template <> struct Stor<ST_FP32> {
     __device__ static void st4_sat_w(c4_t* p, size_t i, float4 v) { p[i] = v; }
     __device__ static float2 ldm(const mom_t* p, size_t i) { return __ldg(p + i); }
     __device__ static void stm(mom_t* p, size_t i, float2 v) { p[i] = v; }
+    // the value ld4 / ldm return after st4 / stm stored v
+    __device__ static float4 rt4(float4 v) { return v; }
+    __device__ static float2 rtm(float2 v) { return v; }
     __device__ static float qin(float v) { return v; }
     // a-trous scratch record (32 B): float4 (r, g, b, var) then the guide float4 (n, z)
     typedef float4 rec_t;
@@ -333,6 +336,9 @@ template <> struct Stor<ST_FP16> {
     }
     __device__ static float2 ldm(const mom_t* p, size_t i) { return unpack_h2(__ldg(p + i)); }
     __device__ static void stm(mom_t* p, size_t i, float2 v) { p[i] = pack_h2(sat16(v.x), sat16(v.y)); }
+    // the value ld4 / ldm return after st4 / stm stored v
+    __device__ static float4 rt4(float4 v) { return unpack_h4(pack_h4(v)); }
+    __device__ static float2 rtm(float2 v) { return unpack_h2(pack_h2(sat16(v.x), sat16(v.y))); }
     __device__ static float qin(float v) { return q16(v); }
     // a-trous scratch record (16 B): half (r, g), half (b, var), octahedral code, z bits
     typedef uint4 rec_t;

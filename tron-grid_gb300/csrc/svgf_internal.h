@@ -35,5 +35,7 @@ size_t rec_bytes_of(const tg_svgf_params& p);
 size_t col_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 // Byte offset of that variance plane from the start of the buffer.
 size_t col_var_offset_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
+// Bytes of the per-pixel-block fallback flags of a FULL frame.
+size_t fb_flags_bytes_of(uint32_t w, uint32_t h);
 
 } // namespace tg

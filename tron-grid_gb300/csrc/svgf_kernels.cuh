@@ -98,6 +98,7 @@ struct FullArgs {
     void* col_dst;
     size_t var_off;         // byte offset of the variance plane in col_src / col_dst
     float2* grad;           // per-pixel depth gradient (written by the temporal kernel)
+    int* fb_flags;          // per 32x8 pixel block: 1 if a pixel needs the spatial variance fallback
     int* err;               // device error word (bounded waits that gave up); may be null
     ResLayout lin, lout;    // scratch layouts of col_src and col_dst
     float alpha, alpha_m, sigma_l, sigma_n, sigma_z;
@@ -107,8 +108,11 @@ struct FullArgs {
 };
 
 // K1: guide write, reprojection (bilinear 2x2 with depth/normal test), history
-// length, colour EMA and mean-centred moment EMA.
-template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArgs& a, int x, int y)
+// length, colour EMA and mean-centred moment EMA.  A pixel whose history is at
+// least `fallback_frames` long also gets its level-0 record (colour, temporal
+// variance, guide) here, from the values as stored; the function returns true
+// for the others, whose variance needs the neighbours' moments (K2).
+template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArgs& a, int x, int y)
 {
     typedef Stor<ST> S;
     typedef typename S::guide_t G;
@@ -120,7 +124,8 @@ template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArg
     float3 n = ld_normal(a.normal, x, y, ST == ST_FP16, enc);
     if (ST == ST_FP16) n = oct16_decode_raw(enc);  // FP16 storage keeps the octahedral code
     const float z = ld_depth(a.depth, x, y);
-    static_cast<G*>(a.guide_cur)[i] = S::mk_guide(n, enc, z);
+    const G gv = S::mk_guide(n, enc, z);
+    static_cast<G*>(a.guide_cur)[i] = gv;
 
     const bool hl = x > 0, hr = x < a.w - 1, hu = y > 0, hd = y < a.h - 1;
     const float gx = grad1(z, hl ? ld_depth(a.depth, x - 1, y) : 0.0f, hr ? ld_depth(a.depth, x + 1, y) : 0.0f, hl, hr);
@@ -220,13 +225,22 @@ template <int ST> __device__ __forceinline__ void full_temporal_px(const FullArg
         mu = l;
         var = 0.0f;
     }
-    S::st4(static_cast<C4*>(a.tc), i, make_float4(orr, og, ob, float(len)));
-    S::stm(static_cast<M*>(a.mom_cur), i, make_float2(mu, var));
+    const float4 tcv = make_float4(orr, og, ob, float(len));
+    const float2 mom = make_float2(mu, var);
+    S::st4(static_cast<C4*>(a.tc), i, tcv);
+    S::stm(static_cast<M*>(a.mom_cur), i, mom);
+    const float4 t = S::rt4(tcv);
+    if (int(t.w) < a.fallback_frames) return true;
+    const float v = S::rtm(mom).y;
+    S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, v), gv);
+    S::st_var(a.col_dst, a.var_off, i, v);
+    return false;
 }
 
-// K2: variance per pixel: the temporal moment variance, or for histories
-// shorter than `fallback_frames` a 7x7 depth/normal-weighted spatial estimate
-// from the neighbours' moments.  Writes col = (colour, variance).
+// K2: for histories shorter than `fallback_frames`, the variance is a 7x7
+// depth/normal-weighted spatial estimate from the neighbours' moments; writes
+// the level-0 record (colour, variance, guide) of such a pixel.  The other
+// pixels' records come from K1.
 template <int ST> __device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y)
 {
     typedef Stor<ST> S;
@@ -239,9 +253,10 @@ template <int ST> __device__ __forceinline__ void full_variance_px(const FullArg
     const G* gc = static_cast<const G*>(a.guide_cur);
     const float4 t = S::ld4(tc, i);
     const int len = int(t.w);
+    if (len >= a.fallback_frames) return;
     const float2 mom = S::ldm(mc, i);
     float var = mom.y;
-    if (len < a.fallback_frames) {
+    {
         const float4 g = S::ld_guide_w(gc, i);
         const float2 gr = a.grad[i];
         // w = max(0, n.n')^sigma_n exp(-|dz| / (sigma_z |grad z . off| + eps_z)), as one ex2
@@ -278,18 +293,33 @@ template <int ST> __device__ __forceinline__ void full_variance_px(const FullArg
     S::st_var(a.col_dst, a.var_off, i, var);
 }
 
+// One kBlockX x kBlockY pixel block `blk` (row-major over the image's blocks)
+// of K1 and K2.  K1 records in fb_flags[blk] whether any pixel of the block
+// needs the spatial fallback; K2 skips the blocks that need none.  Every thread
+// of the CTA calls these (K1 synchronises the CTA).
+template <int ST> __device__ __forceinline__ void full_temporal_block(const FullArgs& a, int blk, int x, int y)
+{
+    const bool fb = (x < a.w && y < a.h) ? full_temporal_px<ST>(a, x, y) : false;
+    const int any = __syncthreads_or(fb);
+    if (threadIdx.x == 0 && threadIdx.y == 0) a.fb_flags[blk] = any;
+}
+
+template <int ST> __device__ __forceinline__ void full_variance_block(const FullArgs& a, int blk, int x, int y)
+{
+    if (__ldcg(a.fb_flags + blk) == 0) return;
+    if (x < a.w && y < a.h) full_variance_px<ST>(a, x, y);
+}
+
 template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY, 4) k_full_temporal(FullArgs a)
 {
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    if (x < a.w && y < a.h) full_temporal_px<ST>(a, x, y);
+    full_temporal_block<ST>(a, blockIdx.y * gridDim.x + blockIdx.x, blockIdx.x * kBlockX + threadIdx.x,
+                            blockIdx.y * kBlockY + threadIdx.y);
 }
 
 template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_variance(FullArgs a)
 {
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    if (x < a.w && y < a.h) full_variance_px<ST>(a, x, y);
+    full_variance_block<ST>(a, blockIdx.y * gridDim.x + blockIdx.x, blockIdx.x * kBlockX + threadIdx.x,
+                            blockIdx.y * kBlockY + threadIdx.y);
 }
 
 } // namespace tg

@@ -65,12 +65,20 @@ template <int R> struct LevelOcc {
 };
 
 // Staged tile of one level: X0 = (r, g, b, variance), X1 = (unit normal, depth),
-// XL = luminance.  X0 and X1 are 128-byte aligned so that a TMA box can land
-// in them directly (N * 16 bytes is a multiple of 128 for both tile shapes).
-template <int R> struct __align__(128) LevelSmem {
+// XL = luminance; FP16 storage also keeps each record's octahedral normal code
+// (XO), which the output record carries on unchanged.  X0 and X1 are 128-byte
+// aligned so that a TMA box can land in them directly (N * 16 bytes is a
+// multiple of 128 for every tile shape used).
+template <int R, int ST> struct __align__(128) LevelSmem {
     float4 X0[LevelTile<R>::N];
     float4 X1[LevelTile<R>::N];
     float XL[LevelTile<R>::N];
+};
+template <int R> struct __align__(128) LevelSmem<R, ST_FP16> {
+    float4 X0[LevelTile<R>::N];
+    float4 X1[LevelTile<R>::N];
+    float XL[LevelTile<R>::N];
+    uint32_t XO[LevelTile<R>::N];
 };
 
 // Maps tile `bid` to (residue a, b) and its tile origin in sub-lattice units.
@@ -113,12 +121,10 @@ __host__ __device__ inline LevelArgs level_args_of(const FullArgs& a)
 // Per-centre values read from global memory before the tile is staged, so
 // that their latency overlaps the staging: the depth gradient, the 3x3
 // variance neighbourhood (contiguous in the residue-major layout: the index of
-// (qx, qy) separates into a column and a row term) and, for FP16 storage, the
-// centre's raw guide that the output record carries on.
+// (qx, qy) separates into a column and a row term).
 template <int ST, int R> struct CentrePre {
     float vn9[R][9];
     float2 gr[R];
-    typename Stor<ST>::graw_t graw[R];
     bool valid[R];
     float kx_sum;
 };
@@ -144,9 +150,6 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
         const int y = rb + s * (j0 + int(threadIdx.y) * R + k);
         pre.valid[k] = cx < a.w && y < a.h;
         pre.gr[k] = pre.valid[k] ? a.grad[y * a.w + cx] : make_float2(0.f, 0.f);
-        if (ST == ST_FP16)
-            pre.graw[k] = pre.valid[k] ? S::ld_graw(static_cast<const typename S::guide_t*>(a.guide_cur), y * a.w + cx)
-                                       : typename S::graw_t{};
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const int qy = y + f - 1;
@@ -173,7 +176,7 @@ __device__ __forceinline__ bool staged_inside(const FullArgs& a, int s, int ra, 
 template <int ST, int R>
 __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra,
                                               int rb, int i0, int j0, const CentrePre<ST, R>& pre,
-                                              const LevelSmem<R>& sm)
+                                              const LevelSmem<R, ST>& sm)
 {
     typedef Stor<ST> S;
     typedef typename S::c4_t C4;
@@ -277,7 +280,7 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
         } else {
             typename S::graw_t graw;
             if constexpr (ST == ST_FP16)
-                graw = pre.graw[k];
+                graw = make_uint2(sm.XO[c], __float_as_uint(sm.X1[c].w));
             else
                 graw = sm.X1[c];
             const size_t oi = res_idx(lv.lout, cx, y);
@@ -292,7 +295,7 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
 // before reusing `sm`.
 template <int ST, int R>
 __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
-                                                LevelSmem<R>& sm)
+                                                LevelSmem<R, ST>& sm)
 {
     typedef Stor<ST> S;
     typedef typename S::rec_t RT;
@@ -307,10 +310,19 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
     const int plane = ((rb << lv.lin.lg) + ra) * P;
     for (int k = threadIdx.y * kLvTX + threadIdx.x; k < T::N; k += kLvTX * kLvRows) {
         float4 c = make_float4(0.f, 0.f, 0.f, 0.f), n = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t oct = 0;
         if (staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
             const int sj = k / T::SW, si = k - sj * T::SW;
-            S::ld_rec(src, plane + (j0 + sj - 2) * pw + (i0 + si - 2), c, n);
+            const size_t ri = plane + (j0 + sj - 2) * pw + (i0 + si - 2);
+            if constexpr (ST == ST_FP16) {
+                const uint4 u = __ldg(src + ri);
+                S::decode_rec(u, c, n);
+                oct = u.z;
+            } else {
+                S::ld_rec(src, ri, c, n);
+            }
         }
+        if constexpr (ST == ST_FP16) sm.XO[k] = oct;
         sm.X0[k] = c;
         sm.X1[k] = n;
         sm.XL[k] = lum(c.x, c.y, c.z);
@@ -321,7 +333,7 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
 
 template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
-    __shared__ LevelSmem<R> sm;
+    __shared__ LevelSmem<R, ST> sm;
     full_level_tile<ST, R>(a, level_args_of(a), g, blockIdx.x, sm);
 }
 
@@ -359,7 +371,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm)
 {
     typedef LevelTile<R> T;
-    __shared__ LevelSmem<R> sm;
+    __shared__ LevelSmem<R, ST> sm;
     __shared__ __align__(8) uint64_t bar;
     // FP16 records (16 B) land in the X1 array and are decoded in place: each
     // thread reads raw record k before it writes X0/X1/XL entry k.
@@ -415,7 +427,9 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
         const bool in = staged_inside<R>(a, s, ra, rb, i0, j0, k);
         float4 c, n;
         if constexpr (ST == ST_FP16) {
-            Stor<ST_FP16>::decode_rec(raw[k], c, n);
+            const uint4 u = raw[k];
+            Stor<ST_FP16>::decode_rec(u, c, n);
+            sm.XO[k] = u.z;
         } else {
             c = sm.X0[k];
             n = sm.X1[k];

@@ -115,6 +115,7 @@ struct Sess {
     void* mom[2];
     void* tc;
     float2* grad;
+    int* fb_flags;
     void* colA;
     void* colB;
     char* state;
@@ -185,7 +186,7 @@ size_t slot_bytes(const tg_svgf_params& p, const Sess& s)
     const bool f16 = p.storage == TG_SVGF_STORAGE_FP16;
     const size_t c4 = f16 ? 8 : 16;
     size_t b = al256(state_bytes_of(p, s.w, s.h));
-    b += al256(np * c4) + al256(np * sizeof(float2)) + 2 * col_bytes_of(p, s.w, s.h);
+    b += al256(np * c4) + al256(np * sizeof(float2)) + al256(fb_flags_bytes_of(s.w, s.h)) + 2 * col_bytes_of(p, s.w, s.h);
     for (int k = 0; k < 4; ++k) b += 2 * al256(in_bytes(s, k));
     b += 2 * al256(size_t(fmt_bytes(s.fmt[4])) * np);
     return b;
@@ -210,6 +211,8 @@ void carve(tg_svgf_server* sv, Sess& s)
     p += al256(np * c4);
     s.grad = reinterpret_cast<float2*>(p);
     p += al256(np * sizeof(float2));
+    s.fb_flags = reinterpret_cast<int*>(p);
+    p += al256(fb_flags_bytes_of(s.w, s.h));
     const size_t colb = col_bytes_of(sv->d.params, s.w, s.h);
     s.colA = p;
     p += colb;
@@ -284,6 +287,7 @@ FullArgs args_for(tg_svgf_server* sv, Sess& s)
     a.mom_cur = s.mom[cur];
     a.tc = s.tc;
     a.grad = s.grad;
+    a.fb_flags = s.fb_flags;
     a.col_dst = s.colA;
     a.var_off = col_var_offset_of(sv->d.params, s.w, s.h);
     const tg_svgf_params& p = sv->d.params;
