@@ -196,6 +196,7 @@ static const char* kFamilyName[kFamilies] = {"ref_init", "ref_level", "full_temp
 
 struct tg_svgf {
     int device = 0;
+    int sms = 1;  // multiprocessors of the device
     uint32_t w = 0, h = 0;
     tg_svgf_params p{};
     uint64_t frame = 0;
@@ -546,10 +547,11 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         });
         // variance: the block flags; the flagged blocks' short-history pixels (data-dependent, not counted)
         launch(s, stream, F_FULL_VARIANCE, double(fb_flags_bytes_of(s->w, s->h)), [&] {
+            const int vg = variance_grid(int(grd.x * grd.y), s->sms);
             if (f16)
-                k_full_variance<ST_FP16><<<grd, blk, 0, stream>>>(a);
+                k_full_variance<ST_FP16><<<vg, blk, 0, stream>>>(a);
             else
-                k_full_variance<ST_FP32><<<grd, blk, 0, stream>>>(a);
+                k_full_variance<ST_FP32><<<vg, blk, 0, stream>>>(a);
         });
         void* src = s->colA;
         void* oth = s->colB;
@@ -672,6 +674,8 @@ int tg_svgf_create(const tg_svgf_desc* desc, tg_svgf** out)
     tg_svgf* s = new (std::nothrow) tg_svgf();
     if (!s) return fail(TG_ERR_OOM, "host allocation failed");
     s->device = dev;
+    cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (s->sms < 1) s->sms = 1;
     s->w = desc->width;
     s->h = desc->height;
     s->p = desc->params;

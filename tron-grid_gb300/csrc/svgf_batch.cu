@@ -255,7 +255,7 @@ void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const 
                 acc += int(level_blocks(level_geom(W, H, 1 << (stage - 2), b->R)));
         }
         pf[n] = acc;
-        b->grids[k][stage] = acc;
+        b->grids[k][stage] = stage == 1 ? variance_grid(acc, b->sm_count) : acc;
     }
     for (uint32_t j = 0; j < n; ++j) {
         tg_svgf_batch::Stream& s = b->st[ids[j]];

@@ -83,8 +83,24 @@ __device__ __forceinline__ bool grid_barrier(BarrierState* b, unsigned nblocks, 
     return ok != 0;
 }
 
-// The persistent kernel runs the pixel stages on its level-shaped CTAs.
+// Stream of work item `item` in a stage's prefix sums pf[0..n].
+__device__ __forceinline__ int find_stream(const int* pf, int n, int item)
+{
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pf[mid] <= item)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// The persistent kernel runs the pixel stages on its level-shaped CTAs, and
+// K2 stages its tile in the level tile's shared memory.
 static_assert(kLvTX == kBlockX && kLvRows == kBlockY, "pixel and level CTAs must have the same shape");
+static_assert(sizeof(VarTile) <= sizeof(LevelSmem<1, ST_FP32>), "K2 tile must fit the level tile");
 
 template <int ST, int R>
 __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __restrict__ table, int cap,
@@ -92,32 +108,46 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
                                                                    long long spin_cycles)
 {
     __shared__ LevelSmem<R, ST> sm;
+    __shared__ VarList vl;
     const BatchHeader hd = *reinterpret_cast<const BatchHeader*>(table);
     const int* prefix = reinterpret_cast<const int*>(table + table_prefix_offset());
     const BatchEntry* ent = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap));
     for (int stage = 0; stage < hd.n_stages; ++stage) {
         const int* pf = prefix + stage * (cap + 1);
         const int items = pf[hd.n];
-        for (int item = blockIdx.x; item < items; item += gridDim.x) {
-            int lo = 0, hi = hd.n;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (pf[mid] <= item)
-                    lo = mid;
-                else
-                    hi = mid;
+        if (stage == 1) {
+            // K2: only the flagged pixel blocks, compacted a chunk at a time
+            for (int base = blockIdx.x; base < items; base += gridDim.x * kVarPerCta) {
+                variance_compact(
+                    base, int(gridDim.x), items,
+                    [&](int it) {
+                        const int j = find_stream(pf, hd.n, it);
+                        return __ldcg(ent[j].fa.fb_flags + (it - pf[j])) != 0;
+                    },
+                    vl);
+                const int n = vl.n;
+                for (int e = 0; e < n; ++e) {
+                    const int it = vl.item[e];
+                    const int j = find_stream(pf, hd.n, it), local = it - pf[j];
+                    const FullArgs& a = ent[j].fa;
+                    const int tx = (a.w + kBlockX - 1) / kBlockX;
+                    full_variance_tile<ST>(a, (local % tx) * kBlockX + threadIdx.x, (local / tx) * kBlockY + threadIdx.y,
+                                           *reinterpret_cast<VarTile*>(&sm));
+                }
+                __syncthreads();  // vl is refilled by the next chunk
             }
+            if (stage + 1 < hd.n_stages && !grid_barrier(bar, expect_blocks, spin_cycles)) return;
+            continue;
+        }
+        for (int item = blockIdx.x; item < items; item += gridDim.x) {
+            const int lo = find_stream(pf, hd.n, item);
             const int local = item - pf[lo];
             const BatchEntry& e = ent[lo];
             const FullArgs& a = e.fa;
-            if (stage < 2) {
+            if (stage == 0) {
                 const int tx = (a.w + kBlockX - 1) / kBlockX;
-                const int x = (local % tx) * kBlockX + threadIdx.x;
-                const int y = (local / tx) * kBlockY + threadIdx.y;
-                if (stage == 0)
-                    full_temporal_block<ST>(a, local, x, y);
-                else
-                    full_variance_block<ST>(a, local, x, y);
+                full_temporal_block<ST>(a, local, (local % tx) * kBlockX + threadIdx.x,
+                                        (local / tx) * kBlockY + threadIdx.y);
             } else {
                 const int L = stage - 2;
                 LevelArgs lv;
@@ -142,36 +172,43 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
 // active streams (the work-list of one stage is the blocks of one grid).  The
 // hardware schedules the blocks; each kernel keeps its own occupancy.
 
-__device__ __forceinline__ int find_stream(const int* pf, int n, int item)
-{
-    int lo = 0, hi = n;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (pf[mid] <= item)
-            lo = mid;
-        else
-            hi = mid;
-    }
-    return lo;
-}
 
+// STAGE 0 (K1): one CTA per pixel block.  STAGE 1 (K2): one chunk of
+// kVarPerCta blocks per CTA (gridDim.x = variance_grid(items, SMs)).
 template <int ST, int STAGE>
 __global__ void __launch_bounds__(kBlockX* kBlockY) k_ms_pixel(const char* __restrict__ table, int cap)
 {
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + STAGE * (cap + 1);
-    const int item = blockIdx.x;
-    if (item >= pf[hd->n]) return;
-    const int j = find_stream(pf, hd->n, item);
-    const int local = item - pf[j];
-    const FullArgs& a = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap))[j].fa;
-    const int tx = (a.w + kBlockX - 1) / kBlockX;
-    const int x = (local % tx) * kBlockX + threadIdx.x;
-    const int y = (local / tx) * kBlockY + threadIdx.y;
-    if (STAGE == 0)
-        full_temporal_block<ST>(a, local, x, y);
-    else
-        full_variance_block<ST>(a, local, x, y);
+    const BatchEntry* ent = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap));
+    const int n_str = hd->n, items = pf[n_str];
+    if constexpr (STAGE == 0) {
+        const int item = blockIdx.x;
+        if (item >= items) return;
+        const int j = find_stream(pf, n_str, item);
+        const int local = item - pf[j];
+        const FullArgs& a = ent[j].fa;
+        const int tx = (a.w + kBlockX - 1) / kBlockX;
+        full_temporal_block<ST>(a, local, (local % tx) * kBlockX + threadIdx.x, (local / tx) * kBlockY + threadIdx.y);
+    } else {
+        __shared__ VarTile vt;
+        __shared__ VarList vl;
+        variance_compact(
+            int(blockIdx.x), int(gridDim.x), items,
+            [&](int it) {
+                const int j = find_stream(pf, n_str, it);
+                return __ldcg(ent[j].fa.fb_flags + (it - pf[j])) != 0;
+            },
+            vl);
+        const int n = vl.n;
+        for (int e = 0; e < n; ++e) {
+            const int it = vl.item[e];
+            const int j = find_stream(pf, n_str, it), local = it - pf[j];
+            const FullArgs& a = ent[j].fa;
+            const int tx = (a.w + kBlockX - 1) / kBlockX;
+            full_variance_tile<ST>(a, (local % tx) * kBlockX + threadIdx.x, (local / tx) * kBlockY + threadIdx.y, vt);
+        }
+    }
 }
 
 template <int ST, int R>

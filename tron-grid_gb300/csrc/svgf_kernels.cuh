@@ -241,55 +241,73 @@ template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArg
 // depth/normal-weighted spatial estimate from the neighbours' moments; writes
 // the level-0 record (colour, variance, guide) of such a pixel.  The other
 // pixels' records come from K1.
-template <int ST> __device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y)
+//
+// A CTA stages the guides (decoded) and moments of its pixel block plus a
+// 3-pixel halo in shared memory.  Cells outside the image hold a zero normal,
+// whose weight max(0, n.n')^sigma_n = 2^(sigma_n lg2 0) is exactly 0, so the
+// sums equal those over the inside neighbours only.
+constexpr int kVarHalo = 3;
+constexpr int kVarTW = kBlockX + 2 * kVarHalo;
+constexpr int kVarTH = kBlockY + 2 * kVarHalo;
+struct VarTile {
+    float4 g[kVarTH * kVarTW];  // unit normal, depth
+    float2 m[kVarTH * kVarTW];  // luminance mean, variance
+};
+
+template <int ST>
+__device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y, int cell, const VarTile& vt)
 {
     typedef Stor<ST> S;
     typedef typename S::guide_t G;
     typedef typename S::c4_t C4;
-    typedef typename S::mom_t M;
     const size_t i = size_t(y) * a.w + x;
-    const C4* tc = static_cast<const C4*>(a.tc);
-    const M* mc = static_cast<const M*>(a.mom_cur);
-    const G* gc = static_cast<const G*>(a.guide_cur);
-    const float4 t = S::ld4(tc, i);
+    const float4 t = S::ld4(static_cast<const C4*>(a.tc), i);
     const int len = int(t.w);
     if (len >= a.fallback_frames) return;
-    const float2 mom = S::ldm(mc, i);
-    float var = mom.y;
-    {
-        const float4 g = S::ld_guide_w(gc, i);
-        const float2 gr = a.grad[i];
-        // w = max(0, n.n')^sigma_n exp(-|dz| / (sigma_z |grad z . off| + eps_z)), as one ex2
-        const float A_ = a.sigma_z * gr.x * (1.0f / kLog2eF), B_ = a.sigma_z * gr.y * (1.0f / kLog2eF);
-        const float ez = kEpsZ * (1.0f / kLog2eF);
-        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
-        for (int dy = -3; dy <= 3; ++dy) {
-            const int qy = y + dy;
-            if (qy < 0 || qy >= a.h) continue;
+    const float2 mom = vt.m[cell];
+    const float4 g = vt.g[cell];
+    const float2 gr = a.grad[i];
+    // w = max(0, n.n')^sigma_n exp(-|dz| / (sigma_z |grad z . off| + eps_z)), as one ex2;
+    // offsets (dx, dy) and (-dx, -dy) share the depth scale kz
+    const float A_ = a.sigma_z * gr.x * (1.0f / kLog2eF), B_ = a.sigma_z * gr.y * (1.0f / kLog2eF);
+    const float ez = kEpsZ * (1.0f / kLog2eF);
+    float kz[25];
 #pragma unroll
-            for (int dx = -3; dx <= 3; ++dx) {
-                const int qx = x + dx;
-                if (qx < 0 || qx >= a.w) continue;
-                const size_t j = size_t(qy) * a.w + qx;
-                const float4 q = S::ld_guide_w(gc, j);
-                const float d = fmaf(q.z, g.z, fmaf(q.y, g.y, q.x * g.x));
-                float t = -fabsf(q.w - g.w) * rcp_approx(fabsf(float(dx) * A_ + float(dy) * B_) + ez);
-                t = fmaf(a.sigma_n, lg2_approx(fmaxf(d, 0.0f)), t);
-                const float wgt = ex2_approx(t);
-                const float2 m = S::ldm(mc, j);
-                const float dm = m.x - mom.x;
-                s0 += wgt;
-                s1 = fmaf(wgt, dm, s1);
-                s2 = fmaf(wgt, fmaf(dm, dm, m.y), s2);
-            }
-        }
-        if (s0 > 0.0f) {
-            const float m1 = s1 / s0;
-            var = fmaxf(0.0f, s2 / s0 - m1 * m1);
+    for (int q = 0; q < 25; ++q) {
+        // q enumerates the offsets with dy < 0, or dy == 0 and dx <= 0 (the centre is q = 24)
+        const int dy = q < 21 ? q / 7 - 3 : 0;
+        const int dx = q < 21 ? q % 7 - 3 : q - 24;
+        kz[q] = rcp_approx(fabsf(fmaf(float(dx), A_, float(dy) * B_)) + ez);
+    }
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+    for (int dy = -kVarHalo; dy <= kVarHalo; ++dy) {
+#pragma unroll
+        for (int dx = -kVarHalo; dx <= kVarHalo; ++dx) {
+            const bool neg = dy < 0 || (dy == 0 && dx <= 0);
+            const int ex = neg ? dx : -dx, ey = neg ? dy : -dy;
+            const int q = ey < 0 ? (ey + 3) * 7 + (ex + 3) : 24 + ex;
+            const int c = cell + dy * kVarTW + dx;
+            const float4 n = vt.g[c];
+            const float d = fmaf(n.z, g.z, fmaf(n.y, g.y, n.x * g.x));
+            float e = -fabsf(n.w - g.w) * kz[q];
+            e = fmaf(a.sigma_n, lg2_approx(fmaxf(d, 0.0f)), e);
+            const float wgt = ex2_approx(e);
+            const float2 m = vt.m[c];
+            const float dm = m.x - mom.x;
+            s0 += wgt;
+            s1 = fmaf(wgt, dm, s1);
+            s2 = fmaf(wgt, fmaf(dm, dm, m.y), s2);
         }
     }
+    float var = mom.y;
+    if (s0 > 0.0f) {
+        const float m1 = s1 / s0;
+        var = fmaxf(0.0f, s2 / s0 - m1 * m1);
+    }
     // level-0 input record: colour + variance, and the pixel's guide for the edge stops
-    S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var), S::ld_graw(gc, i));
+    S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var),
+              S::ld_graw(static_cast<const G*>(a.guide_cur), i));
     S::st_var(a.col_dst, a.var_off, i, var);
 }
 
@@ -304,10 +322,60 @@ template <int ST> __device__ __forceinline__ void full_temporal_block(const Full
     if (threadIdx.x == 0 && threadIdx.y == 0) a.fb_flags[blk] = any;
 }
 
-template <int ST> __device__ __forceinline__ void full_variance_block(const FullArgs& a, int blk, int x, int y)
+// K2 on one flagged pixel block; (x, y) is this thread's pixel of the block.
+template <int ST> __device__ __forceinline__ void full_variance_tile(const FullArgs& a, int x, int y, VarTile& vt)
 {
-    if (__ldcg(a.fb_flags + blk) == 0) return;
-    if (x < a.w && y < a.h) full_variance_px<ST>(a, x, y);
+    typedef Stor<ST> S;
+    const int x0 = x - int(threadIdx.x) - kVarHalo, y0 = y - int(threadIdx.y) - kVarHalo;
+    const typename S::guide_t* gc = static_cast<const typename S::guide_t*>(a.guide_cur);
+    const typename S::mom_t* mc = static_cast<const typename S::mom_t*>(a.mom_cur);
+    for (int k = threadIdx.y * kBlockX + threadIdx.x; k < kVarTH * kVarTW; k += kBlockX * kBlockY) {
+        const int qy = y0 + k / kVarTW, qx = x0 + k % kVarTW;
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 m = make_float2(0.f, 0.f);
+        if (qx >= 0 && qy >= 0 && qx < a.w && qy < a.h) {
+            const size_t j = size_t(qy) * a.w + qx;
+            g = S::ld_guide_w(gc, j);
+            m = S::ldm(mc, j);
+        }
+        vt.g[k] = g;
+        vt.m[k] = m;
+    }
+    __syncthreads();
+    if (x < a.w && y < a.h)
+        full_variance_px<ST>(a, x, y, (int(threadIdx.y) + kVarHalo) * kVarTW + int(threadIdx.x) + kVarHalo, vt);
+    __syncthreads();  // the tile's storage is reused by the caller's next block
+}
+
+// K2 grids: a CTA takes the pixel blocks base + t * stride (t < kVarPerCta) of
+// its chunk, compacts the flagged ones into a shared list and runs only those,
+// so that the mostly unflagged blocks of a frame cost one parallel flag read
+// per chunk instead of one CTA each.
+constexpr int kVarPerCta = 32;
+
+__host__ __device__ inline int variance_grid(int items, int sms)
+{
+    const int lo = (items + kVarPerCta - 1) / kVarPerCta, hi = items < 6 * sms ? items : 6 * sms;
+    return lo > hi ? lo : hi;
+}
+
+struct VarList {
+    int item[kVarPerCta];
+    int n;
+};
+
+// Fills `l` with the flagged items of the chunk at `base`; `flag(item)` reads an item's flag.
+template <class Flag>
+__device__ __forceinline__ void variance_compact(int base, int stride, int items, Flag flag, VarList& l)
+{
+    const int tid = threadIdx.y * kBlockX + threadIdx.x;
+    if (tid == 0) l.n = 0;
+    __syncthreads();
+    if (tid < kVarPerCta) {
+        const int item = base + tid * stride;
+        if (item < items && flag(item)) l.item[atomicAdd(&l.n, 1)] = item;
+    }
+    __syncthreads();
 }
 
 template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY, 4) k_full_temporal(FullArgs a)
@@ -316,10 +384,19 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY, 4) k_full_
                             blockIdx.y * kBlockY + threadIdx.y);
 }
 
+// One chunk per CTA: gridDim.x = variance_grid(blocks, SMs) covers every block.
 template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_variance(FullArgs a)
 {
-    full_variance_block<ST>(a, blockIdx.y * gridDim.x + blockIdx.x, blockIdx.x * kBlockX + threadIdx.x,
-                            blockIdx.y * kBlockY + threadIdx.y);
+    __shared__ VarTile vt;
+    __shared__ VarList l;
+    const int tx = (a.w + kBlockX - 1) / kBlockX, items = tx * ((a.h + kBlockY - 1) / kBlockY);
+    const int* flags = a.fb_flags;
+    variance_compact(int(blockIdx.x), int(gridDim.x), items, [flags](int b) { return __ldcg(flags + b) != 0; }, l);
+    const int n = l.n;
+    for (int e = 0; e < n; ++e) {
+        const int b = l.item[e];
+        full_variance_tile<ST>(a, (b % tx) * kBlockX + threadIdx.x, (b / tx) * kBlockY + threadIdx.y, vt);
+    }
 }
 
 } // namespace tg

@@ -371,7 +371,7 @@ void launch_batch(tg_svgf_server* sv, std::vector<Sess*>& ss, int k)
                 acc += int(level_blocks(level_geom(W, H, 1 << (stage - 2), kR)));
         }
         pf[n] = acc;
-        grids[stage] = acc;
+        grids[stage] = stage == 1 ? variance_grid(acc, sv->sm_count) : acc;
     }
     for (int j = 0; j < n; ++j) {
         ent[j].fa = args_for(sv, *ss[j]);
@@ -410,12 +410,13 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
     const dim3 blk(kBlockX, kBlockY);
     const dim3 grd((s.w + kBlockX - 1) / kBlockX, (s.h + kBlockY - 1) / kBlockY);
     cudaStream_t st = sv->s_comp;
+    const int vg = variance_grid(int(grd.x * grd.y), sv->sm_count);
     if (sv->f16) {
         k_full_temporal<ST_FP16><<<grd, blk, 0, st>>>(a);
-        k_full_variance<ST_FP16><<<grd, blk, 0, st>>>(a);
+        k_full_variance<ST_FP16><<<vg, blk, 0, st>>>(a);
     } else {
         k_full_temporal<ST_FP32><<<grd, blk, 0, st>>>(a);
-        k_full_variance<ST_FP32><<<grd, blk, 0, st>>>(a);
+        k_full_variance<ST_FP32><<<vg, blk, 0, st>>>(a);
     }
     void* src = s.colA;
     void* oth = s.colB;
