@@ -637,14 +637,14 @@ def run_e2e(args, frames, dev, mode, storage, world):
     host = [{k: v.cpu().pin_memory() for k, v in frames[i].items()} for i in range(n_host)]
     W, H = args.width, args.height
     out_dt = torch.float32 if args.storage == "fp32" else torch.float16
-    houts = [torch.empty((H, W, 4), dtype=out_dt, pin_memory=True) for _ in range(2)]
+    houts = [torch.empty((H, W, 4), dtype=out_dt, pin_memory=True) for _ in range(3)]
     den = tg.Denoiser(W, H, mode=mode, storage=storage, device=dev.index)
     h2d = sum(v.numel() * v.element_size() for v in host[0].values())
     d2h = houts[0].numel() * houts[0].element_size()
 
     def step(i):
         fr = host[i % n_host]
-        den.denoise_host(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=houts[i & 1])
+        den.denoise_host(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=houts[i % 3])
 
     for i in range(max(3, min(args.warmup, 8))):
         step(i)
@@ -664,7 +664,7 @@ def run_e2e(args, frames, dev, mode, storage, world):
     den.close()
     return {"value": total / el, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": el / steps * 1e3, "host_frames_cycled": n_host,
-            "api": "tg_svgf_denoise_host (pinned host buffers, double-buffered staging)"}
+            "api": "tg_svgf_denoise_host (pinned host buffers, a ring of three staging sets)"}
 
 
 def run_cpu_baseline(args, spec, seconds=15.0, frames=None):

@@ -170,9 +170,10 @@ TG_API int tg_svgf_denoise(tg_svgf* h, const tg_svgf_inputs* inputs, const tg_sv
 /* As tg_svgf_denoise, with inputs and output in HOST memory.  Copies the inputs
  * to handle-owned device staging, denoises and copies the result back, all
  * ordered after prior work on `stream`; returns before the copies finish.
- * The caller keeps the host buffers alive and unmodified until `stream` is
- * synchronised.  Host buffers should be page-locked for the copies to overlap
- * with compute; the staging is double-buffered so consecutive frames overlap. */
+ * The copies run on the handle's own streams, so the caller keeps the host
+ * buffers alive and unmodified until tg_svgf_synchronize returns.  Host
+ * buffers should be page-locked for the copies to overlap with compute; the
+ * staging is a ring of three sets, so up to three frames are in flight. */
 TG_API int tg_svgf_denoise_host(tg_svgf* h, const tg_svgf_inputs* host_inputs, const tg_svgf_outputs* host_outputs,
                          void* stream);
 

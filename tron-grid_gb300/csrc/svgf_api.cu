@@ -216,13 +216,15 @@ struct tg_svgf {
     int flags = 0;
     bool tma = false;                // a-trous tiles staged by TMA
     CUtensorMap tmaps[10];           // per level: the level's input records
-    // host-call staging (double buffered)
+    // host-call staging: a ring of three sets, so that a frame's upload never
+    // waits for the download of the frame two before it
+    static constexpr int kStaging = 3;
     struct Staging {
         char* buf = nullptr;
         size_t bytes = 0;
         cudaEvent_t ev_in = nullptr, ev_comp = nullptr, ev_done = nullptr;
         bool used = false;
-    } stg[2];
+    } stg[kStaging];
     int stg_next = 0;
     cudaStream_t copy_stream = nullptr;  // host -> device
     cudaStream_t d2h_stream = nullptr;   // device -> host (its own stream, so uploads never queue behind it)
@@ -773,7 +775,7 @@ int tg_svgf_denoise_host(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_out
         return fail(TG_ERR_CUDA, "output copy failed: %s", cudaGetErrorString(cudaGetLastError()));
     if (cudaEventRecord(sg.ev_done, s->d2h_stream) != cudaSuccess) return fail(TG_ERR_CUDA, "event record failed");
     sg.used = true;
-    s->stg_next ^= 1;
+    s->stg_next = (s->stg_next + 1) % tg_svgf::kStaging;
     return TG_OK;
 }
 
@@ -834,7 +836,8 @@ int tg_svgf_get_info(const tg_svgf* s, tg_svgf_info* info)
     info->frame_index = s->frame;
     info->state_bytes = s->state_bytes;
     info->scratch_bytes = s->scratch_bytes;
-    info->staging_bytes = s->stg[0].bytes + s->stg[1].bytes;
+    info->staging_bytes = 0;
+    for (const auto& sg : s->stg) info->staging_bytes += sg.bytes;
     info->kernels_per_frame = uint32_t(s->p.levels + (s->p.mode == TG_SVGF_MODE_FULL ? 2 : 1));
     info->tma = s->tma ? 1u : 0u;
     int e = 0;
