@@ -329,6 +329,7 @@ def run_tg(args, rank, world, local):
         res["ref_exact_720p"] = run_single(args, dev, "ref", "fp16", steps=min(args.steps, 200), size=(1280, 720))
         res["batched"] = run_batched(args, dev)
         res["serving"] = run_serving(args, dev)
+        res["fog_filter"] = run_fog(args, dev, cpu=rank == 0 and world == 1 and not args.no_cpu)
         if rank == 0:
             res["accuracy"] = run_accuracy(dev)
         torch.cuda.empty_cache()
@@ -381,6 +382,77 @@ def run_single(args, dev, mode_s, storage_s, steps, size=None):
             "kernels": {k: {"launches": v["launches"], "avg_ms": v["total_ms"] / max(v["launches"], 1),
                             "gbs": v["algo_bytes"] / max(v["total_ms"], 1e-12) / 1e6} for k, v in prof.items()},
             "workload": f"{'FULL' if mode_s == 'full' else 'REF_EXACT'} {W}x{H} {storage_s.upper()} storage"}
+
+
+def run_fog(args, dev, steps=200, cpu=True):
+    """The volumetric-fog froxel filter (src/volumetric_filter.slang, tg_fog_filter) on rgba16f volumes: the
+    reference's 320x180x64 grid and a 640x360x128 grid, one pass per frame of a 60-frame camera sequence with the
+    (history, output) pair alternating.  Each pass is timed by its own CUDA events with L2 flushed (a 256 MB
+    write) before it; the CPU baseline is the oracle on the host cores at the reference grid."""
+    import numpy as np
+    import torch
+
+    import tron_grid_gb300 as tg
+    from tron_grid_gb300 import fog_scene
+
+    peak, src = load_peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    res = {"workload": "froxel filter, rgba16f inject/history/output, 60-frame camera sequence (yaw 0.5 deg + "
+                       "0.05 m per frame), alpha 0.1, near 0.1 m, far 120 m",
+           "algo_bytes_per_froxel": 24, "l2": "flushed (256 MB write) before every timed pass"}
+    for name, kw in (("reference_grid", {}), ("grid_640x360x128", dict(width=640, height=360, depth=128))):
+        spec = fog_scene.fog_config(**kw)
+        sc = fog_scene.FogScene(spec, device=dev)
+        pool = [sc.inject(t) for t in range(8)]
+        params = [tg.fog_params(**sc.param_args(t)) for t in range(spec.frames)]
+        ff = tg.FogFilter(spec.width, spec.height, spec.depth, device=dev)
+
+        def step(i):
+            t = 1 + i % (spec.frames - 1)
+            ff.step(params[t], pool[t % len(pool)])
+
+        for i in range(5):
+            step(i)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize()
+        for i in range(steps):
+            flush.fill_(i & 255)
+            evs[i][0].record(stream)
+            step(5 + i)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        ms = np.array([a.elapsed_time(b) for a, b in evs])
+        n = spec.width * spec.height * spec.depth
+        avg = float(ms.mean())
+        gbs = 24 * n / (avg / 1e3) / 1e9
+        res[name] = {"froxels": n, "ms_per_pass": avg, "p50_ms": float(np.median(ms)), "p99_ms": float(np.percentile(ms, 99)),
+                     "gfroxels_per_s": n / avg / 1e6, "gpu_launches_per_pass": 1,
+                     "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                                  "peak_source": src}}
+        del pool, ff
+    del flush
+    torch.cuda.empty_cache()
+    if cpu:
+        import oracle
+
+        spec = fog_scene.fog_config()
+        sc = fog_scene.FogScene(spec)
+        hist = np.zeros((spec.depth, spec.height, spec.width, 4), np.float32)
+        done, el = 0, 0.0
+        while el < 5.0 and done < 59:
+            t = 1 + done
+            blk = oracle.fog_param_block(**sc.param_args(t))
+            raw = sc.inject(t).float().numpy()
+            t0 = time.perf_counter()
+            hist = oracle.fog_filter(blk, raw, hist)
+            el += time.perf_counter() - t0
+            done += 1
+        n = spec.width * spec.height * spec.depth
+        res["cpu_baseline"] = {"value": done * n / el / 1e6, "unit": "Mfroxels/s", "ms_per_pass": el / done * 1e3,
+                               "cores": oracle.num_threads(), "kind": "port",
+                               "sample": f"{done} passes of the 320x180x64 sequence (float32, fp16 stores)"}
+    return res
 
 
 def run_batched(args, dev):

@@ -8,6 +8,10 @@ module; the product never imports it.  Arrays are numpy, row-major (h, w, c).
 * ``ref_frame_reference`` - the reference shader source itself compiled as C++
   (oracle/build.py), when the translation could be built.
 * ``full_frame`` - the full Schied-2017 SVGF superset, float32 or float64.
+* ``fog_filter`` - restatement of the volumetric-fog froxel filter
+  (`src/volumetric_filter.slang:142-226`), float32 or float64;
+  ``fog_filter_reference`` - that shader compiled as C++ (oracle/build.py).
+  Froxel volumes are numpy (d, h, w, 4).
 """
 from __future__ import annotations
 
@@ -20,6 +24,7 @@ from . import build as _build
 
 _orc = None
 _ref = None
+_fogref = None
 
 
 class FullParams(C.Structure):
@@ -58,6 +63,7 @@ def _lib():
         _orc.orc_oct16_encode.argtypes = [C.c_int, P, P]
         _orc.orc_oct16_decode.argtypes = [C.c_int, P, P]
         _orc.orc_num_threads.restype = C.c_int
+        _orc.orc_fog_filter.argtypes = [C.c_char_p, P, P, P, C.c_int, C.c_int, C.c_int]
     return _orc
 
 
@@ -169,3 +175,86 @@ def oct16_decode(enc):
     out = np.zeros((e.shape[0], 3), np.float32)
     _lib().orc_oct16_decode(e.shape[0], _p(e), _p(out))
     return out.reshape(tuple(np.shape(enc)[:-1]) + (3,))
+
+
+# ------------------------------------------------------ volumetric-fog filter ----
+
+FOG_PARAM_BYTES = 176
+
+
+def fog_param_block(inv_view_projection, prev_view_projection, camera_pos, alpha, width, height, depth,
+                    history_valid, near_plane, far_plane) -> bytes:
+    """The 176-byte parameter block of the froxel filter (the reference's
+    VolumetricFilterPushConstants layout, `src/main.cpp:221-234`).
+
+    The matrices are given as 4x4 arrays in mathematical order (clip = M @ [x, y, z, 1]) and stored
+    column-major, element (col, row) at index col * 4 + row, as the reference's MathLib::Mat4.
+    """
+    import struct
+
+    def cm(m):
+        m = np.asarray(m, dtype=np.float64).reshape(4, 4)
+        return [float(v) for v in m.T.reshape(16)]
+
+    cam = [float(v) for v in np.asarray(camera_pos, dtype=np.float64).reshape(3)]
+    blk = struct.pack("<16f16f3ff4I4f", *cm(inv_view_projection), *cm(prev_view_projection), *cam, float(alpha),
+                      int(width), int(height), int(depth), int(history_valid), float(near_plane), float(far_plane),
+                      0.0, 0.0)
+    assert len(blk) == FOG_PARAM_BYTES
+    return blk
+
+
+def _fog_dims(block: bytes):
+    import struct
+
+    w, h, d, _ = struct.unpack_from("<4I", block, 36 * 4)
+    return w, h, d
+
+
+def fog_filter(block: bytes, raw, history, fp16_store=True, dtype=np.float32, threads=0):
+    """One froxel-filter pass (restatement).  raw / history (d, h, w, 4) -> out (d, h, w, 4) float32."""
+    w, h, d = _fog_dims(block)
+    raw = _c(raw, np.float32).reshape(d, h, w, 4)
+    history = _c(history, np.float32).reshape(d, h, w, 4)
+    out = np.zeros((d, h, w, 4), np.float32)
+    rc = _lib().orc_fog_filter(block, _p(raw), _p(history), _p(out), int(bool(fp16_store)),
+                               int(dtype == np.float64), threads)
+    if rc:
+        raise ValueError("oracle fog_filter rejected its arguments")
+    return out
+
+
+def fog_reference_available() -> bool:
+    return _fogreflib() is not None
+
+
+def _fogreflib():
+    global _fogref
+    if _fogref is None:
+        path = _build.FOG_REF_LIB
+        if not os.path.exists(path):
+            try:
+                path = _build.build_fog_reference()
+            except Exception:
+                path = None
+        if path is None or not os.path.exists(path):
+            return None
+        _fogref = C.CDLL(path)
+        P = C.c_void_p
+        _fogref.ref_fog_filter.argtypes = [C.c_char_p, P, P, P, C.c_int, C.c_int]
+    return _fogref
+
+
+def fog_filter_reference(block: bytes, raw, history, fp16_store=True, threads=0):
+    """The reference froxel-filter shader itself (compiled as C++)."""
+    lib = _fogreflib()
+    if lib is None:
+        raise RuntimeError("reference froxel-filter translation not built (oracle/_ref)")
+    w, h, d = _fog_dims(block)
+    raw = _c(raw, np.float32).reshape(d, h, w, 4).copy()
+    history = _c(history, np.float32).reshape(d, h, w, 4).copy()
+    out = np.zeros((d, h, w, 4), np.float32)
+    rc = lib.ref_fog_filter(block, _p(raw), _p(history), _p(out), int(bool(fp16_store)), threads)
+    if rc:
+        raise ValueError("reference fog filter rejected its arguments")
+    return out

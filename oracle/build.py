@@ -1,18 +1,24 @@
 """Build recipe for the CPU oracle.  TEST INFRASTRUCTURE ONLY.
 
 Produces
-  oracle/_build/liborc.so   - the C++ restatement (oracle/svgf_oracle.cpp);
+  oracle/_build/liborc.so    - the C++ restatements (oracle/svgf_oracle.cpp,
+                               oracle/fog_oracle.cpp);
   oracle/_ref/libsvgf_ref.so - the reference shader `src/svgf_denoise.slang`
+                               compiled as C++ (when its translation exists);
+  oracle/_ref/libfog_ref.so  - the reference shader `src/volumetric_filter.slang`
                                compiled as C++ (when its translation exists).
 
-The translation of the shader is made here from the reference checkout, with
-exactly three textual edits that remove Slang-only syntax:
+The translations of the shaders are made here from the reference checkout, with
+textual edits that remove Slang-only syntax:
   * the `[shader("compute")]` attribute line,
   * the `[numthreads(8, 8, 1)]` attribute line,
-  * the `: SV_DispatchThreadID` parameter semantic.
-Everything else in the shader compiles unchanged against oracle/slang_prelude.hpp.
-The translation is written to oracle/_ref/ (git-ignored, never committed) so
-that a machine without the reference checkout can still compile it.
+  * the `: SV_DispatchThreadID` parameter semantic,
+and, for the froxel filter, an `f` suffix on every unsuffixed floating literal
+(Slang floating literals are 32-bit; the denoiser's arithmetic is unaffected by
+this and its translation does not need it).  Everything else compiles unchanged
+against oracle/slang_prelude.hpp / oracle/slang_prelude_fog.hpp.  The
+translations are written to oracle/_ref/ (git-ignored, never committed) so that
+a machine without the reference checkout can still compile them.
 
 Usage: python oracle/build.py [--reference-root DIR]
 """
@@ -30,6 +36,8 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORC_LIB = os.path.join(BUILD_DIR, "liborc.so")
 REF_LIB = os.path.join(REF_DIR, "libsvgf_ref.so")
 REF_GEN = os.path.join(REF_DIR, "svgf_denoise_gen.cpp")
+FOG_REF_LIB = os.path.join(REF_DIR, "libfog_ref.so")
+FOG_REF_GEN = os.path.join(REF_DIR, "volumetric_filter_gen.cpp")
 DEFAULT_REFERENCE_ROOT = "/root/reference"
 
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"]
@@ -43,13 +51,65 @@ def _newer(target: str, *sources: str) -> bool:
 
 
 def build_oracle(force: bool = False) -> str:
-    src = os.path.join(HERE, "svgf_oracle.cpp")
+    srcs = [os.path.join(HERE, "svgf_oracle.cpp"), os.path.join(HERE, "fog_oracle.cpp")]
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if force or not _newer(ORC_LIB, src):
+    if force or not _newer(ORC_LIB, *srcs):
         tmp = ORC_LIB + ".tmp"
-        subprocess.check_call(["g++", *CXXFLAGS, src, "-o", tmp])
+        subprocess.check_call(["g++", *CXXFLAGS, *srcs, "-o", tmp])
         os.replace(tmp, ORC_LIB)
     return ORC_LIB
+
+
+_FLOAT_LITERAL = re.compile(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
+
+
+def _strip_slang(text: str, shader: str) -> str:
+    out_lines = []
+    removed = 0
+    for line in text.splitlines():
+        s = line.strip()
+        if s == '[shader("compute")]' or re.fullmatch(r"\[numthreads\(\s*8\s*,\s*8\s*,\s*1\s*\)\]", s):
+            removed += 1
+            continue
+        out_lines.append(line)
+    body = "\n".join(out_lines) + "\n"
+    body, nsem = re.subn(r"\s*:\s*SV_DispatchThreadID", "", body)
+    if removed != 2 or nsem != 1:
+        raise RuntimeError(f"unexpected layout of {shader} (attributes removed={removed}, semantics={nsem})")
+    return body
+
+
+def _write_if_changed(path: str, text: str) -> None:
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    if not os.path.exists(path) or open(path, encoding="utf-8").read() != text:
+        with open(path, "w", encoding="utf-8") as f:
+            f.write(text)
+
+
+def translate_fog_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+    """Write oracle/_ref/volumetric_filter_gen.cpp from the reference shader, if present."""
+    shader = os.path.join(reference_root, "src", "volumetric_filter.slang")
+    if not os.path.isfile(shader):
+        return None
+    with open(shader, encoding="utf-8") as f:
+        body = _strip_slang(f.read(), shader)
+    body = _FLOAT_LITERAL.sub(lambda m: m.group(1) + "f", body)
+    _write_if_changed(FOG_REF_GEN, f"// Generated by oracle/build.py from {shader}; not committed.\n" + body)
+    return FOG_REF_GEN
+
+
+def build_fog_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+    """Compile the translated froxel-filter shader; None when no translation exists."""
+    translate_fog_reference(reference_root)
+    if not os.path.isfile(FOG_REF_GEN):
+        return None
+    drv = os.path.join(HERE, "fog_ref_driver.cpp")
+    pre = os.path.join(HERE, "slang_prelude_fog.hpp")
+    if force or not _newer(FOG_REF_LIB, FOG_REF_GEN, drv, pre):
+        tmp = FOG_REF_LIB + ".tmp"
+        subprocess.check_call(["g++", *CXXFLAGS, "-std=c++20", "-Wno-attributes", "-I", HERE, "-I", REF_DIR, drv, "-o", tmp])
+        os.replace(tmp, FOG_REF_LIB)
+    return FOG_REF_LIB
 
 
 def translate_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
@@ -102,6 +162,8 @@ def main(argv=None) -> int:
     print(build_oracle(a.force))
     r = build_reference(a.force, a.reference_root)
     print(r if r else "reference shader translation absent: oracle/_ref not built")
+    r = build_fog_reference(a.force, a.reference_root)
+    print(r if r else "reference froxel-filter translation absent: oracle/_ref/libfog_ref.so not built")
     return 0
 
 

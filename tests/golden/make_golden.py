@@ -1,9 +1,11 @@
-"""Generates tests/golden/ref_exact_*.npz from the reference shader itself.
+"""Generates tests/golden/ref_exact_*.npz and tests/golden/fog_*.npz from the
+reference shaders themselves.
 
-The reference shader `src/svgf_denoise.slang` is compiled as C++ by
-oracle/build.py (three Slang-only tokens removed, everything else unchanged)
-and run here on seeded inputs; its outputs are the golden vectors that pin the
-oracle's restatement on machines without the reference checkout.
+The reference shaders `src/svgf_denoise.slang` and `src/volumetric_filter.slang`
+are compiled as C++ by oracle/build.py (the Slang-only tokens removed,
+floating literals of the froxel filter suffixed as float, everything else
+unchanged) and run here on seeded inputs; their outputs are the golden vectors
+that pin the oracle's restatements on machines without the reference checkout.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout)
 """
@@ -19,6 +21,43 @@ import oracle  # noqa: E402
 
 CASES = [(33, 17, 5, 0), (8, 8, 3, 1), (1, 1, 4, 2), (2, 3, 4, 3), (64, 36, 4, 4)]
 
+# froxel-filter sequences: (w, h, d, frames, seed, yaw deg/frame, translation m/frame); frame 0 has no history.
+# The second case's camera turns 90 deg per frame (most froxels fall outside the previous grid or behind the
+# previous camera); the third moves 150 m per frame along its view axis (previous depth beyond far).
+FOG_CASES = [(24, 14, 8, 4, 0, 3.0, (0.2, 0.0, -0.5)), (9, 5, 3, 3, 1, 90.0, (0.0, 0.0, 0.0)),
+             (16, 9, 6, 3, 2, 0.0, (0.0, 0.0, -150.0)), (1, 1, 1, 2, 3, 1.0, (0.0, 0.0, -0.1))]
+
+
+def fog_sequence(w, h, d, frames, seed, yaw, trans):
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "tron-grid_gb300"))
+    import fog_scene  # noqa: E402
+
+    sc = fog_scene.FogScene(fog_scene.FogSpec(width=w, height=h, depth=d, yaw_deg=yaw, translation=trans,
+                                              seed=seed, frames=frames))
+    rng = np.random.default_rng(100 + seed)
+    blocks, raws = [], []
+    for t in range(frames):
+        blocks.append(np.frombuffer(oracle.fog_param_block(**sc.param_args(t)), np.uint8))
+        raw = rng.uniform(0.0, 2.0, size=(d, h, w, 4)) * rng.exponential(1.0, size=(d, h, w, 1))
+        raws.append(raw.astype(np.float16).astype(np.float32))
+    return np.stack(blocks), np.stack(raws)
+
+
+def make_fog():
+    for (w, h, d, frames, seed, yaw, trans) in FOG_CASES:
+        blocks, raw = fog_sequence(w, h, d, frames, seed, yaw, trans)
+        rec = {"params": blocks, "raw": raw}
+        for f16 in (True, False):
+            hist = np.zeros((d, h, w, 4), np.float32)
+            outs = []
+            for t in range(frames):
+                hist = oracle.fog_filter_reference(blocks[t].tobytes(), raw[t], hist, fp16_store=f16)
+                outs.append(hist)
+            rec[f"out_{'f16' if f16 else 'f32'}"] = np.stack(outs)
+        path = os.path.join(HERE, f"fog_{w}x{h}x{d}_s{seed}.npz")
+        np.savez_compressed(path, **rec)
+        print(path, os.path.getsize(path))
+
 
 def inputs(w, h, frames, seed):
     rng = np.random.default_rng(seed)
@@ -32,9 +71,10 @@ def inputs(w, h, frames, seed):
 
 
 def main():
-    if not oracle.reference_available():
+    if not oracle.reference_available() or not oracle.fog_reference_available():
         print("reference shader translation unavailable; nothing generated")
         return 1
+    make_fog()
     for (w, h, frames, seed) in CASES:
         raw = inputs(w, h, frames, seed)
         rec = {"raw": raw}

@@ -1,4 +1,4 @@
-"""ctypes declarations of include/tg_svgf.h and the loader of libtg_svgf.so.
+"""ctypes declarations of include/tg_svgf.h, include/tg_fog.h and the loader of libtg_svgf.so.
 
 The library is the product: if it is missing the import of this package fails
 with an error that says how to build it.  There is no CPU fallback.
@@ -101,6 +101,19 @@ class TgError(RuntimeError):
         self.status = status
 
 
+class FogParams(C.Structure):
+    """tg_fog_filter_params: the reference's 176-byte VolumetricFilterPushConstants layout."""
+    _fields_ = [("inv_view_projection", C.c_float * 16), ("prev_view_projection", C.c_float * 16),
+                ("camera_pos", C.c_float * 3), ("alpha", C.c_float), ("froxel_width", C.c_uint32),
+                ("froxel_height", C.c_uint32), ("froxel_depth", C.c_uint32), ("history_valid", C.c_uint32),
+                ("near_plane", C.c_float), ("far_plane", C.c_float), ("pad0", C.c_float), ("pad1", C.c_float)]
+
+
+class Volume(C.Structure):
+    _fields_ = [("ptr", C.c_void_p), ("row_pitch_bytes", C.c_int64), ("slice_pitch_bytes", C.c_int64),
+                ("format", C.c_int32), ("reserved", C.c_int32)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/*.h.
 _P = C.c_void_p
 SIGNATURES = {
@@ -136,6 +149,7 @@ SIGNATURES = {
     "tg_svgf_server_destroy": (None, [_P]),
     "tg_svgf_denoise_ref_noalloc": (C.c_int, [C.POINTER(Params), C.c_uint32, C.c_uint32, C.POINTER(Image),
                                               C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), _P]),
+    "tg_fog_filter": (C.c_int, [C.POINTER(FogParams), C.POINTER(Volume), C.POINTER(Volume), C.POINTER(Volume), _P]),
 }
 
 _lib = None
