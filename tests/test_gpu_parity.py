@@ -183,6 +183,37 @@ def test_reset_restarts_history(cuda_dev):
     d.close()
 
 
+@pytest.mark.parametrize("storage", [tg.STORAGE_FP32, tg.STORAGE_FP16])
+def test_resize_rezeroes_state(cuda_dev, storage):
+    """After resize (the reference's rebuildFrameBuffers, src/main.cpp:1547-1603) a handle behaves exactly as a
+    fresh one of the new size; the caller's two outputs alternate as denoised_indirect[frame % 2]."""
+    small = _frames(scene.config1(64, 48, seed=12), 2)
+    big = _frames(scene.config1(96, 80, seed=13), 3)
+    f16 = storage == tg.STORAGE_FP16
+
+    def ins(fr):
+        t = [fr[k].to(cuda_dev) for k in KEYS]
+        if f16:
+            t[0] = t[0].half()
+            t[2] = scene.oct16_encode(t[2])
+        return t
+
+    dt = torch.float16 if f16 else torch.float32
+    d = tg.Denoiser(64, 48, storage=storage)
+    for fr in small:
+        d.denoise(*ins(fr))
+    d.resize(96, 80)
+    fresh = tg.Denoiser(96, 80, storage=storage)
+    outs = [torch.empty((80, 96, 4), dtype=dt, device=cuda_dev) for _ in range(2)]
+    for t, fr in enumerate(big):
+        a = d.denoise(*ins(fr), out=outs[t % 2])
+        b = fresh.denoise(*ins(fr), out=torch.empty_like(outs[0]))
+        assert torch.equal(a.cpu(), b.cpu()), f"frame {t}"
+    assert d.info()["frame_index"] == 3
+    d.close()
+    fresh.close()
+
+
 def test_input_layouts_agree(cuda_dev):
     """RGB32F vs RGBA32F vs pitched normals and pitched radiance give identical output."""
     W, H = 48, 40
