@@ -330,6 +330,7 @@ def run_tg(args, rank, world, local):
         res["batched"] = run_batched(args, dev)
         res["serving"] = run_serving(args, dev)
         res["fog_filter"] = run_fog(args, dev, cpu=rank == 0 and world == 1 and not args.no_cpu)
+        res["bloom_post"] = run_post(args, dev, cpu=rank == 0 and world == 1 and not args.no_cpu)
         if rank == 0:
             res["accuracy"] = run_accuracy(dev)
         torch.cuda.empty_cache()
@@ -452,6 +453,70 @@ def run_fog(args, dev, steps=200, cpu=True):
         res["cpu_baseline"] = {"value": done * n / el / 1e6, "unit": "Mfroxels/s", "ms_per_pass": el / done * 1e3,
                                "cores": oracle.num_threads(), "kind": "port",
                                "sample": f"{done} passes of the 320x180x64 sequence (float32, fp16 stores)"}
+    return res
+
+
+def run_post(args, dev, steps=200, cpu=True):
+    """The bloom + post-process chain (src/bloom_downsample.slang, src/postprocess.slang; tg_post_process): rgba16f
+    HDR in, B8G8R8A8 display image out, at 3840x2160 and at the reference's published 1280x720.  HDR frames are the
+    4K sequence's noisy radiance (emitters up to 20 bloom); L2 is flushed (a 256 MB write) before every timed frame,
+    each frame timed by its own CUDA events.  Compulsory bytes: HDR read 8 + display write 4 = 12 B/px (the bloom
+    chain is scratch).  The CPU baseline is the oracle on the host cores at 4K."""
+    import numpy as np
+    import torch
+
+    import tron_grid_gb300 as tg
+    from tron_grid_gb300 import scene
+
+    peak, src = load_peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    res = {"workload": "bloom extract + downsample + upsample mip chain (threshold 1.0, 6 mips) and post-process "
+                       "(chromatic aberration, bloom 0.095, ACES, sRGB, grade, vignette), rgba16f HDR -> BGRA8",
+           "algo_bytes_per_px": 12, "l2": "flushed (256 MB write) before every timed frame"}
+    hdr4k = None
+    for name, (W, H) in (("3840x2160", (3840, 2160)), ("1280x720", (1280, 720))):
+        sc = scene.PlaneScene(scene.config1(W, H, seed=0), device=dev)
+        pool = [sc.frame(t)["radiance"].to(torch.float16).contiguous() for t in range(4)]
+        if hdr4k is None:
+            hdr4k = pool[0].float().cpu().numpy()
+        pp = tg.PostProcessor(W, H, device=dev.index)
+        out = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+        for i in range(5):
+            pp.process(pool[i % 4], out)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize()
+        for i in range(steps):
+            flush.fill_(i & 255)
+            evs[i][0].record(stream)
+            pp.process(pool[i % 4], out)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        ms = np.array([a.elapsed_time(b) for a, b in evs])
+        avg = float(ms.mean())
+        gbs = 12 * W * H / (avg / 1e3) / 1e9
+        res[name] = {"ms_per_frame": avg, "p50_ms": float(np.median(ms)), "mpx_per_s": W * H / avg / 1e3,
+                     "mip_count": pp.info()["mip_count"], "gpu_launches_per_frame": 2 * pp.info()["mip_count"],
+                     "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                                  "peak_source": src}}
+        pp.close()
+        del pool
+    res["1280x720"]["reference_published_ms"] = {"bloom_down": 0.025, "bloom_up": 0.020, "post": 0.029,
+                                                 "note": "debug build, RTX 4090 Laptop (TODO.md:1483-1488)"}
+    del flush
+    torch.cuda.empty_cache()
+    if cpu:
+        import oracle
+
+        done, el = 0, 0.0
+        while el < 4.0 and done < 20:
+            t0 = time.perf_counter()
+            oracle.post_frame(hdr4k)
+            el += time.perf_counter() - t0
+            done += 1
+        res["cpu_baseline"] = {"value": done / el, "unit": "frames/s", "ms_per_frame": el / done * 1e3,
+                               "cores": oracle.num_threads(), "kind": "port",
+                               "sample": f"{done} frames of 3840x2160 (float32 arithmetic, fp16 bloom, UNORM8 output)"}
     return res
 
 

@@ -60,7 +60,9 @@ typedef enum tg_format {
     TG_FMT_RGB32F = 4,  /* 3 x float32 (12 B/px): unit normal */
     TG_FMT_OCT16 = 5,   /* 2 x snorm16 octahedral unit normal (4 B/px) */
     TG_FMT_RG32F = 6,   /* 2 x float32: motion vector */
-    TG_FMT_RG16F = 7    /* 2 x binary16: motion vector */
+    TG_FMT_RG16F = 7,   /* 2 x binary16: motion vector */
+    TG_FMT_RGBA8 = 8,   /* 4 x 8-bit UNORM, R first (4 B/px) */
+    TG_FMT_BGRA8 = 9    /* 4 x 8-bit UNORM, B first: the reference's B8G8R8A8_UNORM swapchain */
 } tg_format;
 
 typedef struct tg_image {

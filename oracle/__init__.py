@@ -12,6 +12,10 @@ module; the product never imports it.  Arrays are numpy, row-major (h, w, c).
   (`src/volumetric_filter.slang:142-226`), float32 or float64;
   ``fog_filter_reference`` - that shader compiled as C++ (oracle/build.py).
   Froxel volumes are numpy (d, h, w, 4).
+* ``post_frame`` - restatement of the bloom + post-process chain
+  (`src/bloom_downsample.slang`, `src/postprocess.slang`, host order
+  `src/main.cpp:306-430`); ``post_frame_reference`` - those shaders compiled
+  as C++.
 """
 from __future__ import annotations
 
@@ -25,6 +29,7 @@ from . import build as _build
 _orc = None
 _ref = None
 _fogref = None
+_postref = None
 
 
 class FullParams(C.Structure):
@@ -64,6 +69,9 @@ def _lib():
         _orc.orc_oct16_decode.argtypes = [C.c_int, P, P]
         _orc.orc_num_threads.restype = C.c_int
         _orc.orc_fog_filter.argtypes = [C.c_char_p, P, P, P, C.c_int, C.c_int, C.c_int]
+        _orc.orc_post_frame.argtypes = [C.c_int, C.c_int, P, C.c_float, C.c_float, C.c_int, P, P, C.c_int, C.c_int,
+                                        C.c_int, C.c_int]
+        _orc.orc_post_frame.restype = C.c_int
     return _orc
 
 
@@ -258,3 +266,75 @@ def fog_filter_reference(block: bytes, raw, history, fp16_store=True, threads=0)
     if rc:
         raise ValueError("reference fog filter rejected its arguments")
     return out
+
+
+# ------------------------------------------------------ bloom + post-process ----
+
+def bloom_mip_sizes(width, height, max_mips=6):
+    """Mip sizes of the bloom image (half the frame, at least 1x1; `src/main.cpp:271-278, 1298-1301`)."""
+    import math
+
+    bw, bh = max(width // 2, 1), max(height // 2, 1)
+    n = min(int(math.floor(math.log2(float(np.float32(max(bw, bh)))))) + 1, max_mips)
+    return [(max(bw >> i, 1), max(bh >> i, 1)) for i in range(n)]
+
+
+def _split_mips(flat, sizes):
+    out, o = [], 0
+    for (w, h) in sizes:
+        out.append(flat[o:o + w * h * 4].reshape(h, w, 4))
+        o += w * h * 4
+    return out
+
+
+def post_frame(hdr, threshold=1.0, strength=0.095, max_mips=6, fp16_store=True, unorm8=True, dtype=np.float32,
+               threads=0):
+    """One frame of the chain (restatement).  hdr (h, w, 4) -> (out (h, w, 4) float32, [bloom mips])."""
+    hdr = _c(hdr, np.float32)
+    h, w = hdr.shape[:2]
+    sizes = bloom_mip_sizes(w, h, max_mips)
+    out = np.zeros((h, w, 4), np.float32)
+    mips = np.zeros(sum(a * b * 4 for a, b in sizes), np.float32)
+    n = _lib().orc_post_frame(w, h, _p(hdr), threshold, strength, max_mips, _p(out), _p(mips), int(bool(fp16_store)),
+                              int(bool(unorm8)), int(dtype == np.float64), threads)
+    if n != len(sizes):
+        raise ValueError("oracle post_frame rejected its arguments")
+    return out, _split_mips(mips, sizes)
+
+
+def post_reference_available() -> bool:
+    return _postreflib() is not None
+
+
+def _postreflib():
+    global _postref
+    if _postref is None:
+        path = _build.POST_REF_LIB
+        if not os.path.exists(path):
+            try:
+                path = _build.build_post_reference()
+            except Exception:
+                path = None
+        if path is None or not os.path.exists(path):
+            return None
+        _postref = C.CDLL(path)
+        P = C.c_void_p
+        _postref.ref_post_frame.argtypes = [C.c_int, C.c_int, P, C.c_float, C.c_float, C.c_int, P, P, C.c_int]
+        _postref.ref_post_frame.restype = C.c_int
+    return _postref
+
+
+def post_frame_reference(hdr, threshold=1.0, strength=0.095, max_mips=6, threads=0):
+    """The reference bloom + post-process shaders themselves (compiled as C++): rgba16f bloom, UNORM8 output."""
+    lib = _postreflib()
+    if lib is None:
+        raise RuntimeError("reference bloom / post-process translation not built (oracle/_ref)")
+    hdr = _c(hdr, np.float32)
+    h, w = hdr.shape[:2]
+    sizes = bloom_mip_sizes(w, h, max_mips)
+    out = np.zeros((h, w, 4), np.float32)
+    mips = np.zeros(sum(a * b * 4 for a, b in sizes), np.float32)
+    n = lib.ref_post_frame(w, h, _p(hdr), threshold, strength, max_mips, _p(out), _p(mips), threads)
+    if n != len(sizes):
+        raise ValueError("reference post frame rejected its arguments")
+    return out, _split_mips(mips, sizes)

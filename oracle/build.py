@@ -6,17 +6,20 @@ Produces
   oracle/_ref/libsvgf_ref.so - the reference shader `src/svgf_denoise.slang`
                                compiled as C++ (when its translation exists);
   oracle/_ref/libfog_ref.so  - the reference shader `src/volumetric_filter.slang`
-                               compiled as C++ (when its translation exists).
+                               compiled as C++ (when its translation exists);
+  oracle/_ref/libpost_ref.so - the reference shaders `src/bloom_downsample.slang`
+                               and `src/postprocess.slang` compiled as C++.
 
 The translations of the shaders are made here from the reference checkout, with
 textual edits that remove Slang-only syntax:
   * the `[shader("compute")]` attribute line,
   * the `[numthreads(8, 8, 1)]` attribute line,
   * the `: SV_DispatchThreadID` parameter semantic,
-and, for the froxel filter, an `f` suffix on every unsuffixed floating literal
-(Slang floating literals are 32-bit; the denoiser's arithmetic is unaffected by
-this and its translation does not need it).  Everything else compiles unchanged
-against oracle/slang_prelude.hpp / oracle/slang_prelude_fog.hpp.  The
+and, for the froxel filter and the bloom / post-process shaders, an `f` suffix
+on every unsuffixed floating literal (Slang floating literals are 32-bit; the
+denoiser's arithmetic is unaffected by this and its translation does not need
+it).  Everything else compiles unchanged against oracle/slang_prelude.hpp,
+oracle/slang_prelude_fog.hpp or oracle/slang_prelude_post.hpp.  The
 translations are written to oracle/_ref/ (git-ignored, never committed) so that
 a machine without the reference checkout can still compile them.
 
@@ -38,6 +41,9 @@ REF_LIB = os.path.join(REF_DIR, "libsvgf_ref.so")
 REF_GEN = os.path.join(REF_DIR, "svgf_denoise_gen.cpp")
 FOG_REF_LIB = os.path.join(REF_DIR, "libfog_ref.so")
 FOG_REF_GEN = os.path.join(REF_DIR, "volumetric_filter_gen.cpp")
+POST_REF_LIB = os.path.join(REF_DIR, "libpost_ref.so")
+BLOOM_REF_GEN = os.path.join(REF_DIR, "bloom_downsample_gen.cpp")
+PP_REF_GEN = os.path.join(REF_DIR, "postprocess_gen.cpp")
 DEFAULT_REFERENCE_ROOT = "/root/reference"
 
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"]
@@ -51,7 +57,7 @@ def _newer(target: str, *sources: str) -> bool:
 
 
 def build_oracle(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, "svgf_oracle.cpp"), os.path.join(HERE, "fog_oracle.cpp")]
+    srcs = [os.path.join(HERE, "svgf_oracle.cpp"), os.path.join(HERE, "fog_oracle.cpp"), os.path.join(HERE, "post_oracle.cpp")]
     os.makedirs(BUILD_DIR, exist_ok=True)
     if force or not _newer(ORC_LIB, *srcs):
         tmp = ORC_LIB + ".tmp"
@@ -63,7 +69,7 @@ def build_oracle(force: bool = False) -> str:
 _FLOAT_LITERAL = re.compile(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
 
 
-def _strip_slang(text: str, shader: str) -> str:
+def _strip_slang(text: str, shader: str, entries: int = 1) -> str:
     out_lines = []
     removed = 0
     for line in text.splitlines():
@@ -74,7 +80,7 @@ def _strip_slang(text: str, shader: str) -> str:
         out_lines.append(line)
     body = "\n".join(out_lines) + "\n"
     body, nsem = re.subn(r"\s*:\s*SV_DispatchThreadID", "", body)
-    if removed != 2 or nsem != 1:
+    if removed != 2 * entries or nsem != entries:
         raise RuntimeError(f"unexpected layout of {shader} (attributes removed={removed}, semantics={nsem})")
     return body
 
@@ -96,6 +102,33 @@ def translate_fog_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str
     body = _FLOAT_LITERAL.sub(lambda m: m.group(1) + "f", body)
     _write_if_changed(FOG_REF_GEN, f"// Generated by oracle/build.py from {shader}; not committed.\n" + body)
     return FOG_REF_GEN
+
+
+def translate_post_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> bool:
+    """Write oracle/_ref/{bloom_downsample,postprocess}_gen.cpp from the reference shaders, if present."""
+    for name, gen, entries in (("bloom_downsample.slang", BLOOM_REF_GEN, 3), ("postprocess.slang", PP_REF_GEN, 1)):
+        shader = os.path.join(reference_root, "src", name)
+        if not os.path.isfile(shader):
+            return False
+        with open(shader, encoding="utf-8") as f:
+            body = _strip_slang(f.read(), shader, entries)
+        body = _FLOAT_LITERAL.sub(lambda m: m.group(1) + "f", body)
+        _write_if_changed(gen, f"// Generated by oracle/build.py from {shader}; not committed.\n" + body)
+    return True
+
+
+def build_post_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+    """Compile the translated bloom / post-process shaders; None when no translation exists."""
+    translate_post_reference(reference_root)
+    if not (os.path.isfile(BLOOM_REF_GEN) and os.path.isfile(PP_REF_GEN)):
+        return None
+    drv = os.path.join(HERE, "post_ref_driver.cpp")
+    pre = os.path.join(HERE, "slang_prelude_post.hpp")
+    if force or not _newer(POST_REF_LIB, BLOOM_REF_GEN, PP_REF_GEN, drv, pre):
+        tmp = POST_REF_LIB + ".tmp"
+        subprocess.check_call(["g++", *CXXFLAGS, "-std=c++20", "-Wno-attributes", "-I", HERE, "-I", REF_DIR, drv, "-o", tmp])
+        os.replace(tmp, POST_REF_LIB)
+    return POST_REF_LIB
 
 
 def build_fog_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
@@ -164,6 +197,8 @@ def main(argv=None) -> int:
     print(r if r else "reference shader translation absent: oracle/_ref not built")
     r = build_fog_reference(a.force, a.reference_root)
     print(r if r else "reference froxel-filter translation absent: oracle/_ref/libfog_ref.so not built")
+    r = build_post_reference(a.force, a.reference_root)
+    print(r if r else "reference bloom / post-process translation absent: oracle/_ref/libpost_ref.so not built")
     return 0
 
 

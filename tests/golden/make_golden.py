@@ -1,11 +1,12 @@
-"""Generates tests/golden/ref_exact_*.npz and tests/golden/fog_*.npz from the
-reference shaders themselves.
+"""Generates tests/golden/ref_exact_*.npz, tests/golden/fog_*.npz and
+tests/golden/post_*.npz from the reference shaders themselves.
 
-The reference shaders `src/svgf_denoise.slang` and `src/volumetric_filter.slang`
-are compiled as C++ by oracle/build.py (the Slang-only tokens removed,
-floating literals of the froxel filter suffixed as float, everything else
-unchanged) and run here on seeded inputs; their outputs are the golden vectors
-that pin the oracle's restatements on machines without the reference checkout.
+The reference shaders `src/svgf_denoise.slang`, `src/volumetric_filter.slang`,
+`src/bloom_downsample.slang` and `src/postprocess.slang` are compiled as C++ by
+oracle/build.py (the Slang-only tokens removed, floating literals of the
+later three suffixed as float, everything else unchanged) and run here on
+seeded inputs; their outputs are the golden vectors that pin the oracle's
+restatements on machines without the reference checkout.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout)
 """
@@ -43,6 +44,28 @@ def fog_sequence(w, h, d, frames, seed, yaw, trans):
     return np.stack(blocks), np.stack(raws)
 
 
+# bloom + post-process frames: (w, h, seed); HDR with sparse bright pixels above the bloom threshold
+POST_CASES = [(1, 1, 0), (3, 5, 1), (64, 36, 2), (97, 61, 3), (160, 90, 4)]
+
+
+def post_hdr(w, h, seed):
+    rng = np.random.default_rng(200 + seed)
+    base = rng.uniform(0.0, 1.2, size=(h, w, 3)) * rng.choice([1.0, 1.0, 1.0, 10.0], size=(h, w, 1))
+    return np.concatenate([base, np.ones((h, w, 1))], -1).astype(np.float16)
+
+
+def make_post():
+    for (w, h, seed) in POST_CASES:
+        hdr = post_hdr(w, h, seed)
+        out, mips = oracle.post_frame_reference(hdr.astype(np.float32))
+        rec = {"hdr": hdr, "out_u8": np.rint(out * 255.0).astype(np.uint8)}
+        for i, m in enumerate(mips):
+            rec[f"mip{i}"] = m.astype(np.float16)
+        path = os.path.join(HERE, f"post_{w}x{h}_s{seed}.npz")
+        np.savez_compressed(path, **rec)
+        print(path, os.path.getsize(path))
+
+
 def make_fog():
     for (w, h, d, frames, seed, yaw, trans) in FOG_CASES:
         blocks, raw = fog_sequence(w, h, d, frames, seed, yaw, trans)
@@ -71,9 +94,10 @@ def inputs(w, h, frames, seed):
 
 
 def main():
-    if not oracle.reference_available() or not oracle.fog_reference_available():
+    if not (oracle.reference_available() and oracle.fog_reference_available() and oracle.post_reference_available()):
         print("reference shader translation unavailable; nothing generated")
         return 1
+    make_post()
     make_fog()
     for (w, h, frames, seed) in CASES:
         raw = inputs(w, h, frames, seed)

@@ -1,4 +1,4 @@
-"""ctypes declarations of include/tg_svgf.h, include/tg_fog.h and the loader of libtg_svgf.so.
+"""ctypes declarations of include/tg_svgf.h, include/tg_fog.h, include/tg_post.h and the loader of libtg_svgf.so.
 
 The library is the product: if it is missing the import of this package fails
 with an error that says how to build it.  There is no CPU fallback.
@@ -14,8 +14,9 @@ LIB_PATH = os.path.join(PKG, "lib", "libtg_svgf.so")
 # tg_status
 OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_BUDGET, ERR_UNSUPPORTED, ERR_STATE = range(8)
 # tg_format
-FMT_NONE, FMT_RGBA32F, FMT_RGBA16F, FMT_R32F, FMT_RGB32F, FMT_OCT16, FMT_RG32F, FMT_RG16F = range(8)
-FMT_BYTES = {FMT_RGBA32F: 16, FMT_RGBA16F: 8, FMT_R32F: 4, FMT_RGB32F: 12, FMT_OCT16: 4, FMT_RG32F: 8, FMT_RG16F: 4}
+FMT_NONE, FMT_RGBA32F, FMT_RGBA16F, FMT_R32F, FMT_RGB32F, FMT_OCT16, FMT_RG32F, FMT_RG16F, FMT_RGBA8, FMT_BGRA8 = range(10)
+FMT_BYTES = {FMT_RGBA32F: 16, FMT_RGBA16F: 8, FMT_R32F: 4, FMT_RGB32F: 12, FMT_OCT16: 4, FMT_RG32F: 8, FMT_RG16F: 4,
+             FMT_RGBA8: 4, FMT_BGRA8: 4}
 # tg_svgf_mode / tg_svgf_storage
 MODE_REF_EXACT, MODE_FULL = 0, 1
 BATCH_STAGES, BATCH_PERSISTENT = 0, 1
@@ -114,6 +115,17 @@ class Volume(C.Structure):
                 ("format", C.c_int32), ("reserved", C.c_int32)]
 
 
+class PostParams(C.Structure):
+    _fields_ = [("bloom_threshold", C.c_float), ("bloom_strength", C.c_float), ("max_mips", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class PostInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("mip_count", C.c_uint32), ("reserved0", C.c_uint32),
+                ("bloom_bytes", C.c_uint64), ("mip_width", C.c_uint32 * 16), ("mip_height", C.c_uint32 * 16),
+                ("mip_ptr", C.c_void_p * 16)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/*.h.
 _P = C.c_void_p
 SIGNATURES = {
@@ -150,6 +162,12 @@ SIGNATURES = {
     "tg_svgf_denoise_ref_noalloc": (C.c_int, [C.POINTER(Params), C.c_uint32, C.c_uint32, C.POINTER(Image),
                                               C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), _P]),
     "tg_fog_filter": (C.c_int, [C.POINTER(FogParams), C.POINTER(Volume), C.POINTER(Volume), C.POINTER(Volume), _P]),
+    "tg_post_params_default": (C.c_int, [C.POINTER(PostParams)]),
+    "tg_post_create": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(PostParams), C.c_int, C.POINTER(_P)]),
+    "tg_post_process": (C.c_int, [_P, C.POINTER(Image), C.POINTER(Image), _P]),
+    "tg_post_resize": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "tg_post_get_info": (C.c_int, [_P, C.POINTER(PostInfo)]),
+    "tg_post_destroy": (None, [_P]),
 }
 
 _lib = None

@@ -46,6 +46,8 @@ int fmt_bytes(int fmt)
     case TG_FMT_OCT16: return 4;
     case TG_FMT_RG32F: return 8;
     case TG_FMT_RG16F: return 4;
+    case TG_FMT_RGBA8: return 4;
+    case TG_FMT_BGRA8: return 4;
     default: return 0;
     }
 }
