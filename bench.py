@@ -331,6 +331,7 @@ def run_tg(args, rank, world, local):
         res["serving"] = run_serving(args, dev)
         res["fog_filter"] = run_fog(args, dev, cpu=rank == 0 and world == 1 and not args.no_cpu)
         res["bloom_post"] = run_post(args, dev, cpu=rank == 0 and world == 1 and not args.no_cpu)
+        res["eye_readback"] = run_eye(args, dev, cpu=rank == 0 and world == 1 and not args.no_cpu)
         if rank == 0:
             res["accuracy"] = run_accuracy(dev)
         torch.cuda.empty_cache()
@@ -517,6 +518,74 @@ def run_post(args, dev, steps=200, cpu=True):
         res["cpu_baseline"] = {"value": done / el, "unit": "frames/s", "ms_per_frame": el / done * 1e3,
                                "cores": oracle.num_threads(), "kind": "port",
                                "sample": f"{done} frames of 3840x2160 (float32 arithmetic, fp16 bloom, UNORM8 output)"}
+    return res
+
+
+def run_eye(args, dev, steps=200, cpu=True):
+    """Eye-frame readback for AI entities (tg_eye_*; the reference's designed vision path, docs/AI_INTERFACE.md):
+    every entity's BGRA8 display image + float32 depth packed as RGB888 + depth into a device slot, copied into a
+    3-slot page-locked host ring, read two frames behind.  `gpu_ms_per_frame`: CUDA events around each frame's pack
+    + copy; `frames_per_s`: the C API driven in a loop (image arrays built once), each submit followed by the
+    acquire of frame t - 2, until the last frame lands in host memory.  Bytes to host = 7 per eye pixel."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import tron_grid_gb300 as tg
+    from tron_grid_gb300 import _lib as L
+
+    lib = L.load()
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    res = {"workload": "N eyes of BGRA8 colour + R32F depth -> RGB888 + float32 depth, 3-slot page-locked host ring"}
+    for name, (n, w, h) in (("64x(64x64)", (64, 64, 64)), ("256x(128x128)", (256, 128, 128))):
+        g = torch.Generator(device="cpu").manual_seed(n)
+        cols = [torch.randint(0, 256, (h, w, 4), generator=g, dtype=torch.uint8).to(dev) for _ in range(n)]
+        deps = [torch.rand((h, w), generator=g).to(dev) for _ in range(n)]
+        er = tg.EyeReadback([(w, h)] * n, fovs=[1.57] * n, device=dev.index)
+        ci = (L.Image * n)(*[L.Image(c.data_ptr(), w * 4, L.FMT_BGRA8, 0) for c in cols])
+        di = (L.Image * n)(*[L.Image(d.data_ptr(), w * 4, L.FMT_R32F, 0) for d in deps])
+        vis = (L.VisionData * n)()
+
+        def step(t):
+            L.check(lib.tg_eye_submit(er.handle, t, ci, di, sp))
+            if t >= 2:
+                L.check(lib.tg_eye_acquire(er.handle, t - 2, vis))
+
+        for t in range(5):
+            step(t)
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            evs[i][0].record(stream)
+            L.check(lib.tg_eye_submit(er.handle, 5 + i, ci, di, sp))
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        gpu_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+        base = 5 + steps
+        t0 = time.perf_counter()
+        for i in range(steps):
+            step(base + i)
+        L.check(lib.tg_eye_acquire(er.handle, base + steps - 1, vis))
+        el = time.perf_counter() - t0
+        bytes_frame = n * w * h * 7
+        res[name] = {"frames_per_s": steps / el, "ms_per_frame": el / steps * 1e3, "gpu_ms_per_frame": gpu_ms,
+                     "host_gbs": bytes_frame / (gpu_ms / 1e3) / 1e9, "bytes_per_frame": bytes_frame,
+                     "gpu_launches_per_frame": 1}
+        if cpu:
+            import oracle
+
+            hc = [c.cpu().numpy() for c in cols]
+            hd = [d.cpu().numpy() for d in deps]
+            t0 = time.perf_counter()
+            reps = 5
+            for _ in range(reps):
+                for c, d in zip(hc, hd):
+                    oracle.eye_pack(c, d)
+            res[name]["cpu_baseline"] = {"ms_per_frame": (time.perf_counter() - t0) / reps * 1e3, "cores": 1,
+                                         "kind": "port", "sample": f"{reps} frames, numpy packing of host copies"}
+        er.close()
     return res
 
 

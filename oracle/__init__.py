@@ -16,6 +16,7 @@ module; the product never imports it.  Arrays are numpy, row-major (h, w, c).
   (`src/bloom_downsample.slang`, `src/postprocess.slang`, host order
   `src/main.cpp:306-430`); ``post_frame_reference`` - those shaders compiled
   as C++.
+* ``eye_pack`` - the eye-frame packing (RGB888 + float32 depth; numpy).
 """
 from __future__ import annotations
 
@@ -338,3 +339,18 @@ def post_frame_reference(hdr, threshold=1.0, strength=0.095, max_mips=6, threads
     if n != len(sizes):
         raise ValueError("reference post frame rejected its arguments")
     return out, _split_mips(mips, sizes)
+
+
+# ------------------------------------------------------------ eye readback ----
+
+def eye_pack(colour, depth, order="bgra"):
+    """The eye frame a brain reads (docs/AI_INTERFACE.md:368-381): RGB888 (h, w, 3) and depth (h, w) float32.
+    colour is (h, w, 4) uint8 (BGRA or RGBA) or float (clamped to [0, 1], scaled by 255 in float32 and rounded
+    to nearest, ties to even)."""
+    colour = np.asarray(colour)
+    if colour.dtype == np.uint8:
+        rgb = colour[..., [2, 1, 0]] if order == "bgra" else colour[..., :3]
+    else:
+        c = np.clip(colour[..., :3].astype(np.float32), np.float32(0), np.float32(1))
+        rgb = np.rint(c * np.float32(255)).astype(np.uint8)
+    return np.ascontiguousarray(rgb), np.asarray(depth, np.float32).copy()

@@ -1,4 +1,4 @@
-"""ctypes declarations of include/tg_svgf.h, include/tg_fog.h, include/tg_post.h and the loader of libtg_svgf.so.
+"""ctypes declarations of include/tg_svgf.h, tg_fog.h, tg_post.h, tg_eye.h and the loader of libtg_svgf.so.
 
 The library is the product: if it is missing the import of this package fails
 with an error that says how to build it.  There is no CPU fallback.
@@ -126,6 +126,17 @@ class PostInfo(C.Structure):
                 ("mip_ptr", C.c_void_p * 16)]
 
 
+class VisionData(C.Structure):
+    _fields_ = [("rgb", C.POINTER(C.c_uint8)), ("depth", C.POINTER(C.c_float)), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("fov_horizontal", C.c_double)]
+
+
+class EyeDesc(C.Structure):
+    _fields_ = [("n_eyes", C.c_uint32), ("widths", C.POINTER(C.c_uint32)), ("heights", C.POINTER(C.c_uint32)),
+                ("fov_horizontal", C.POINTER(C.c_double)), ("ring", C.c_uint32), ("device", C.c_int),
+                ("host_buffer", C.c_void_p), ("host_bytes", C.c_uint64)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/*.h.
 _P = C.c_void_p
 SIGNATURES = {
@@ -168,6 +179,11 @@ SIGNATURES = {
     "tg_post_resize": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "tg_post_get_info": (C.c_int, [_P, C.POINTER(PostInfo)]),
     "tg_post_destroy": (None, [_P]),
+    "tg_eye_host_bytes": (C.c_uint64, [C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32]),
+    "tg_eye_create": (C.c_int, [C.POINTER(EyeDesc), C.POINTER(_P)]),
+    "tg_eye_submit": (C.c_int, [_P, C.c_uint64, C.POINTER(Image), C.POINTER(Image), _P]),
+    "tg_eye_acquire": (C.c_int, [_P, C.c_uint64, C.POINTER(VisionData)]),
+    "tg_eye_destroy": (None, [_P]),
 }
 
 _lib = None
