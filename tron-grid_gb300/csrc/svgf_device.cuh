@@ -79,6 +79,9 @@ __device__ __forceinline__ float dot3_rn(float ax, float ay, float az, float bx,
     return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
 }
 
+// Hint: bring the line holding p towards L2 (no register result; p must lie in an allocation).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 __device__ __forceinline__ float q16(float v) { return __half2float(__float2half_rn(v)); }
 __device__ __forceinline__ float sat16(float v) { return fminf(fmaxf(v, -kHalfMax), kHalfMax); }
 

@@ -119,6 +119,11 @@ template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArg
     typedef typename S::c4_t C4;
     typedef typename S::mom_t M;
     const size_t i = size_t(y) * a.w + x;
+    // The reprojection taps land next to (x, y) under small motion: start their lines towards L2 now, so the
+    // gathers that depend on the motion load find them there instead of paying a second DRAM round trip.
+    prefetch_l2(static_cast<const C4*>(a.hist_prev) + i);
+    prefetch_l2(static_cast<const G*>(a.guide_prev) + i);
+    prefetch_l2(static_cast<const M*>(a.mom_prev) + i);
 
     uint32_t enc = 0;
     float3 n = ld_normal(a.normal, x, y, ST == ST_FP16, enc);
