@@ -59,6 +59,9 @@ def parse_args(argv=None):
     ap.add_argument("--serve-sessions", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-rate", type=float, default=4000.0)
+    ap.add_argument("--only", choices=("fog", "post", "eye"), default=None,
+                    help="run one widening line alone (froxel filter, bloom + post-process, eye readback) for --steps "
+                         "timed frames and print its JSON; one GPU")
     return ap.parse_args(argv)
 
 
@@ -955,6 +958,14 @@ def run_reference(args, rank, world):
 
 def main(argv=None):
     args = parse_args(argv)
+    if args.only is not None:
+        import torch
+
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        fn = {"fog": run_fog, "post": run_post, "eye": run_eye}[args.only]
+        print(json.dumps({args.only: fn(args, dev, steps=args.steps, cpu=not args.no_cpu)}), flush=True)
+        return
     rank, world, local = dist_setup()
     if args.impl == "reference":
         res = run_reference(args, rank, world)
