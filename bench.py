@@ -500,7 +500,8 @@ def run_post(args, dev, steps=200, cpu=True):
         avg = float(ms.mean())
         gbs = 12 * W * H / (avg / 1e3) / 1e9
         res[name] = {"ms_per_frame": avg, "p50_ms": float(np.median(ms)), "mpx_per_s": W * H / avg / 1e3,
-                     "mip_count": pp.info()["mip_count"], "gpu_launches_per_frame": 2 * pp.info()["mip_count"],
+                     "mip_count": pp.info()["mip_count"],
+                     "gpu_launches_per_frame": 1 + max(0, pp.info()["mip_count"] - 6) + pp.info()["mip_count"],
                      "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                                   "peak_source": src}}
         pp.close()

@@ -2,11 +2,12 @@
 //
 // The reference's bloomExtractMain / bloomDownsampleMain / bloomUpsampleMain
 // (src/bloom_downsample.slang) and postprocessMain (src/postprocess.slang),
-// sequenced as the reference host does (src/main.cpp:306-430): extract into
-// mip 0, downsample into mips 1..N-1, upsample mip N-2 .. 0 in place (each
-// texel reads the next mip and its own value, so no texel is read after
-// another thread writes it), then the post pass.  The bloom chain is one
-// allocation of rgba16f mips (8 B per texel, as the reference's bloom image).
+// in the reference host's order (src/main.cpp:306-430): extract into mip 0 and
+// downsample into mips 1..N-1 (one launch builds mips 0..5: each CTA owns an
+// aligned tile of every level), upsample mip N-2 .. 0 in place (each texel
+// reads the next mip and its own value, so no texel is read after another
+// thread writes it), then the post pass.  The bloom chain is one allocation of
+// rgba16f mips (8 B per texel, as the reference's bloom image).
 //
 // All arithmetic is explicitly rounded IEEE single precision in the shaders'
 // order (sums left to right, no contraction into FMA); only the sRGB curve's
@@ -70,12 +71,14 @@ struct Mip {
     int w, h;
 };
 
-template <bool HDR16>
-__global__ void __launch_bounds__(kPostTX* kPostTY)
-    k_bloom_extract(const char* hdr, long long pitch, int W, int H, Mip d, float thr)
+__device__ __forceinline__ C3 round16(C3 c)
 {
-    const int x = blockIdx.x * kPostTX + threadIdx.x, y = blockIdx.y * kPostTY + threadIdx.y;
-    if (x >= d.w || y >= d.h) return;
+    return {__half2float(__float2half_rn(c.r)), __half2float(__float2half_rn(c.g)), __half2float(__float2half_rn(c.b))};
+}
+
+// Mip-0 texel (x, y) of the extraction (bloomExtractMain), before the fp16 store.
+template <bool HDR16> __device__ __forceinline__ C3 extract_texel(const char* hdr, long long pitch, int W, int H, int x, int y, float thr)
+{
     C3 s[4];
     float w[4];
 #pragma unroll
@@ -92,7 +95,71 @@ __global__ void __launch_bounds__(kPostTX* kPostTY)
     auto acc = [&](float C3::*m) {
         return dv(add(add(add(mul(s[0].*m, w[0]), mul(s[1].*m, w[1])), mul(s[2].*m, w[2])), mul(s[3].*m, w[3])), den);
     };
-    st_h4(d.p, (long long)y * d.w + x, {acc(&C3::r), acc(&C3::g), acc(&C3::b)});
+    return {acc(&C3::r), acc(&C3::g), acc(&C3::b)};
+}
+
+// Mip i of the box-downsample chain from the 2x2 block of mip i-1 (bloomDownsampleMain).
+__device__ __forceinline__ C3 box4(const C3 (&c)[4])
+{
+    return {mul(add(add(add(c[0].r, c[1].r), c[2].r), c[3].r), 0.25f), mul(add(add(add(c[0].g, c[1].g), c[2].g), c[3].g), 0.25f),
+            mul(add(add(add(c[0].b, c[1].b), c[2].b), c[3].b), 0.25f)};
+}
+
+// Extraction and the downsample pyramid in one launch.  Mip i texel (x, y) reads exactly the 2x2 block
+// (2x, 2y) .. (2x+1, 2y+1) of mip i-1 (clamped, and the clamp never leaves the block's aligned tile because
+// mip i is floor(mip i-1 / 2) wide, or 1 wide when mip i-1 is), so a CTA that owns an aligned 32x32 tile of
+// mip 0 owns the (32 >> i)-square tile of every mip i <= 5 and builds it from shared memory, with the values
+// as the fp16 image stores them.
+constexpr int kPyrT = 32;
+constexpr int kPyrLevels = 6;
+struct MipSet {
+    Mip m[kPyrLevels];
+    int n;  // levels built here, 1 .. kPyrLevels
+};
+
+template <bool HDR16>
+__global__ void __launch_bounds__(256) k_bloom_pyramid(const char* hdr, long long pitch, int W, int H, MipSet ms, float thr)
+{
+    __shared__ float sa[3][kPyrT * kPyrT];  // ping-pong tiles of one mip level, one plane per channel
+    __shared__ float sb[3][kPyrT * kPyrT];
+    const int tid = threadIdx.x;
+    const int X0 = blockIdx.x * kPyrT, Y0 = blockIdx.y * kPyrT;
+    for (int k = tid; k < kPyrT * kPyrT; k += 256) {
+        const int x = X0 + k % kPyrT, y = Y0 + k / kPyrT;
+        if (x >= ms.m[0].w || y >= ms.m[0].h) continue;
+        const C3 c = round16(extract_texel<HDR16>(hdr, pitch, W, H, x, y, thr));
+        st_h4(ms.m[0].p, (long long)y * ms.m[0].w + x, c);
+        sa[0][k] = c.r;
+        sa[1][k] = c.g;
+        sa[2][k] = c.b;
+    }
+    float(*cur)[kPyrT * kPyrT] = sa;
+    float(*nxt)[kPyrT * kPyrT] = sb;
+    int side = kPyrT;
+    for (int i = 1; i < ms.n; ++i) {
+        __syncthreads();
+        const Mip s = ms.m[i - 1], d = ms.m[i];
+        const int ns = side >> 1, sx0 = X0 >> (i - 1), sy0 = Y0 >> (i - 1), dx0 = X0 >> i, dy0 = Y0 >> i;
+        for (int k = tid; k < ns * ns; k += 256) {
+            const int x = dx0 + k % ns, y = dy0 + k / ns;
+            if (x >= d.w || y >= d.h) continue;
+            C3 c[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = (min(2 * y + (q >> 1), s.h - 1) - sy0) * side + (min(2 * x + (q & 1), s.w - 1) - sx0);
+                c[q] = {cur[0][j], cur[1][j], cur[2][j]};
+            }
+            const C3 v = round16(box4(c));
+            st_h4(d.p, (long long)y * d.w + x, v);
+            nxt[0][k] = v.r;
+            nxt[1][k] = v.g;
+            nxt[2][k] = v.b;
+        }
+        float(*t)[kPyrT * kPyrT] = cur;
+        cur = nxt;
+        nxt = t;
+        side = ns;
+    }
 }
 
 __global__ void __launch_bounds__(kPostTX* kPostTY) k_bloom_down(Mip s, Mip d)
@@ -103,9 +170,7 @@ __global__ void __launch_bounds__(kPostTX* kPostTY) k_bloom_down(Mip s, Mip d)
 #pragma unroll
     for (int k = 0; k < 4; ++k)
         c[k] = ld_h4(s.p, (long long)min(2 * y + (k >> 1), s.h - 1) * s.w + min(2 * x + (k & 1), s.w - 1));
-    st_h4(d.p, (long long)y * d.w + x,
-          {mul(add(add(add(c[0].r, c[1].r), c[2].r), c[3].r), 0.25f), mul(add(add(add(c[0].g, c[1].g), c[2].g), c[3].g), 0.25f),
-           mul(add(add(add(c[0].b, c[1].b), c[2].b), c[3].b), 0.25f)});
+    st_h4(d.p, (long long)y * d.w + x, box4(c));
 }
 
 __global__ void __launch_bounds__(kPostTX* kPostTY) k_bloom_up(Mip s, Mip d)
@@ -318,11 +383,16 @@ int tg_post_process(tg_post* s, const tg_image* hdr, const tg_image* out, void* 
     const char* hb = static_cast<const char*>(hdr->ptr);
     const bool h16 = hdr->format == TG_FMT_RGBA16F;
     const int W = int(s->w), H = int(s->h);
+    // extraction + mips 1..5 in one launch; mips beyond the sixth (max_mips > 6) one launch each
+    MipSet ms;
+    ms.n = std::min(s->n, kPyrLevels);
+    for (int i = 0; i < ms.n; ++i) ms.m[i] = s->mip[i];
+    const dim3 pgrid((s->mip[0].w + kPyrT - 1) / kPyrT, (s->mip[0].h + kPyrT - 1) / kPyrT);
     if (h16)
-        k_bloom_extract<true><<<grid(s->mip[0].w, s->mip[0].h), blk, 0, cs>>>(hb, hp, W, H, s->mip[0], s->p.bloom_threshold);
+        k_bloom_pyramid<true><<<pgrid, 256, 0, cs>>>(hb, hp, W, H, ms, s->p.bloom_threshold);
     else
-        k_bloom_extract<false><<<grid(s->mip[0].w, s->mip[0].h), blk, 0, cs>>>(hb, hp, W, H, s->mip[0], s->p.bloom_threshold);
-    for (int i = 1; i < s->n; ++i) k_bloom_down<<<grid(s->mip[i].w, s->mip[i].h), blk, 0, cs>>>(s->mip[i - 1], s->mip[i]);
+        k_bloom_pyramid<false><<<pgrid, 256, 0, cs>>>(hb, hp, W, H, ms, s->p.bloom_threshold);
+    for (int i = kPyrLevels; i < s->n; ++i) k_bloom_down<<<grid(s->mip[i].w, s->mip[i].h), blk, 0, cs>>>(s->mip[i - 1], s->mip[i]);
     for (int i = s->n - 2; i >= 0; --i) k_bloom_up<<<grid(s->mip[i].w, s->mip[i].h), blk, 0, cs>>>(s->mip[i + 1], s->mip[i]);
     char* ob = static_cast<char*>(out->ptr);
     const float str = s->p.bloom_strength;
