@@ -42,7 +42,8 @@ __device__ __forceinline__ constexpr float log2_b3(int i)
 }
 
 struct LevelGeom {
-    int s;        // stride
+    int s;        // stride, a power of two
+    int lg;       // log2(s)
     int sub_w;    // ceil(W / s): sub-lattice columns of residue 0
     int sub_h;    // ceil(H / s)
     int tiles_x;  // ceil(sub_w / TX)
@@ -82,16 +83,19 @@ template <int R> struct __align__(128) LevelSmem<R, ST_FP16> {
 };
 
 // Maps tile `bid` to (residue a, b) and its tile origin in sub-lattice units.
+// The residue is the low 2 lg bits of the id (s is a power of two), so only
+// the tile row needs a division.
 __device__ __forceinline__ void level_block(const LevelGeom& g, int bid, int TX, int TY, int& ra, int& rb, int& i0,
                                             int& j0)
 {
-    const int ss = g.s * g.s;
-    const int res = bid % ss;
-    const int tile = bid / ss;
-    ra = res % g.s;
-    rb = res / g.s;
-    i0 = (tile % g.tiles_x) * TX;
-    j0 = (tile / g.tiles_x) * TY;
+    const unsigned u = unsigned(bid);
+    const unsigned res = u & ((1u << (2 * g.lg)) - 1u);
+    const unsigned tile = u >> (2 * g.lg);
+    ra = int(res & unsigned(g.s - 1));
+    rb = int(res >> g.lg);
+    const unsigned ty = tile / unsigned(g.tiles_x);
+    i0 = int(tile - ty * unsigned(g.tiles_x)) * TX;
+    j0 = int(ty) * TY;
 }
 
 // ------------------------------------------------------------------ FULL ----
@@ -529,6 +533,8 @@ __host__ __device__ inline LevelGeom level_geom(int w, int h, int s, int R)
 {
     LevelGeom g;
     g.s = s;
+    g.lg = 0;
+    while ((1 << g.lg) < s) ++g.lg;
     g.sub_w = (w + s - 1) / s;
     g.sub_h = (h + s - 1) / s;
     g.tiles_x = (g.sub_w + kLvTX - 1) / kLvTX;
