@@ -293,10 +293,13 @@ template <> struct Stor<ST_FP32> {
         p[2 * i + 1] = g;
     }
     // variance plane beside the records (`off` bytes after the buffer start), 4 B per record
-    __device__ static float ld_var(const void* buf, size_t off, size_t i)
+    typedef float var_t;
+    __device__ static const var_t* var_ptr(const void* buf, size_t off)
     {
-        return __ldg(reinterpret_cast<const float*>(static_cast<const char*>(buf) + off) + i);
+        return reinterpret_cast<const float*>(static_cast<const char*>(buf) + off);
     }
+    __device__ static float var_at(const var_t* p, int i) { return __ldg(p + i); }
+    __device__ static float ld_var(const void* buf, size_t off, size_t i) { return __ldg(var_ptr(buf, off) + i); }
     __device__ static void st_var(void* buf, size_t off, size_t i, float v)
     {
         reinterpret_cast<float*>(static_cast<char*>(buf) + off)[i] = v;
@@ -361,10 +364,13 @@ template <> struct Stor<ST_FP16> {
         p[i] = make_uint4(pack_h2(c.x, c.y), pack_h2(c.z, sat16(c.w)), g.x, g.y);
     }
     // variance plane beside the records, 2 B per record: the same half as the record's
-    __device__ static float ld_var(const void* buf, size_t off, size_t i)
+    typedef unsigned short var_t;
+    __device__ static const var_t* var_ptr(const void* buf, size_t off)
     {
-        return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(static_cast<const char*>(buf) + off) + i)));
+        return reinterpret_cast<const unsigned short*>(static_cast<const char*>(buf) + off);
     }
+    __device__ static float var_at(const var_t* p, int i) { return __half2float(__ushort_as_half(__ldg(p + i))); }
+    __device__ static float ld_var(const void* buf, size_t off, size_t i) { return var_at(var_ptr(buf, off), int(i)); }
     __device__ static void st_var(void* buf, size_t off, size_t i, float v)
     {
         reinterpret_cast<unsigned short*>(static_cast<char*>(buf) + off)[i] = __half_as_ushort(__float2half_rn(sat16(v)));

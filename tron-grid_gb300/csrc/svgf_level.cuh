@@ -149,6 +149,16 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
         cxo[e] = (qx & m) * P + (qx >> lg);
     }
     pre.kx_sum = (cxv[0] ? 0.25f : 0.f) + (cxv[1] ? 0.5f : 0.f) + (cxv[2] ? 0.25f : 0.f);
+    // Every output row y = rb + s jj of this thread has residue rb, so neighbour row y + f - 1 lies in plane row
+    // (rb + f - 1) mod s at position jj + floor((rb + f - 1) / s): its offset is a per-thread constant plus jj pw.
+    const int j_base = (j0 + int(threadIdx.y) * R) * pw;
+    int rowf[3];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        const int t = rb + f - 1;
+        rowf[f] = ((t & m) << lg) * P + (t >> lg) * pw + j_base;
+    }
+    const typename S::var_t* vp = S::var_ptr(lv.col_src, lv.var_off);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int y = rb + s * (j0 + int(threadIdx.y) * R + k);
@@ -156,11 +166,10 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
         pre.gr[k] = pre.valid[k] ? a.grad[y * a.w + cx] : make_float2(0.f, 0.f);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-            const int qy = y + f - 1;
-            const bool oy = pre.valid[k] && unsigned(qy) < unsigned(a.h);
-            const int ro = ((qy & m) << lg) * P + (qy >> lg) * pw;
+            const bool oy = pre.valid[k] && unsigned(y + f - 1) < unsigned(a.h);
 #pragma unroll
-            for (int e = 0; e < 3; ++e) pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::ld_var(lv.col_src, lv.var_off, ro + cxo[e]) : 0.f;
+            for (int e = 0; e < 3; ++e)
+                pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::var_at(vp, rowf[f] + k * pw + cxo[e]) : 0.f;
         }
     }
 }
