@@ -919,10 +919,11 @@ def run_reference(args, rank, world):
     spec, name = workload(args)
     import oracle
 
-    # Each step is one frame of the same sequence on all host threads; the step
-    # count is bounded so that the run ends within a few minutes.
+    # Each step is one frame of the same sequence on all host threads (about a
+    # second at 4K); steps and warm-up frames are bounded so that the run ends
+    # within a few minutes.
     steps = max(1, min(args.steps, 10))
-    warm = max(0, min(args.warmup, 1))
+    warm = max(0, min(args.warmup, 3))
     if warm:
         run_cpu_baseline(args, spec, seconds=0.0, frames=warm)
     base = run_cpu_baseline(args, spec, seconds=0.0, frames=steps)
