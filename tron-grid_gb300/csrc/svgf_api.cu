@@ -573,17 +573,17 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             const double lb = rb + vb + 8 + (a.last ? ob : rb + vb) + (lv == 0 ? 2 * c4 : 0);
             const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
             const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
+            // the last level writes only colour: its kernels leave out the variance propagation
             launch(s, stream, F_FULL_LEVEL, npx * lb, [&] {
                 if (s->tma) {
                     const LevelArgs la = level_args_of(a);
-                    if (f16)
-                        k_full_level_tma<ST_FP16, kLevelR><<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv]);
-                    else
-                        k_full_level_tma<ST_FP32, kLevelR><<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv]);
-                } else if (f16) {
-                    k_full_level_tiled<ST_FP16, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
+                    auto k = f16 ? (a.last ? k_full_level_tma<ST_FP16, kLevelR, false> : k_full_level_tma<ST_FP16, kLevelR, true>)
+                                 : (a.last ? k_full_level_tma<ST_FP32, kLevelR, false> : k_full_level_tma<ST_FP32, kLevelR, true>);
+                    k<<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv]);
                 } else {
-                    k_full_level_tiled<ST_FP32, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
+                    auto k = f16 ? (a.last ? k_full_level_tiled<ST_FP16, kLevelR, false> : k_full_level_tiled<ST_FP16, kLevelR, true>)
+                                 : (a.last ? k_full_level_tiled<ST_FP32, kLevelR, false> : k_full_level_tiled<ST_FP32, kLevelR, true>);
+                    k<<<lgrid, lblk, 0, stream>>>(a, lg);
                 }
             });
             void* t = src;

@@ -186,7 +186,9 @@ __device__ __forceinline__ bool staged_inside(const FullArgs& a, int s, int ra, 
 }
 
 // Everything after staging: per-centre set-up, the taps, the output records.
-template <int ST, int R>
+// VAR = false leaves out the variance propagation (sum of w^2 var): the last
+// level writes only colour.
+template <int ST, int R, bool VAR = true>
 __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra,
                                               int rb, int i0, int j0, const CentrePre<ST, R>& pre,
                                               const LevelSmem<R, ST>& sm)
@@ -263,7 +265,7 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
                     ag[k] = fmaf(w, A.y, ag[k]);
                     ab[k] = fmaf(w, A.z, ab[k]);
                     aw[k] += w;
-                    av[k] = fmaf(w * w, A.w, av[k]);
+                    if constexpr (VAR) av[k] = fmaf(w * w, A.w, av[k]);
                 }
             }
         }
@@ -306,7 +308,7 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
 // One tile of one level, staged with plain coalesced loads (the residue-major
 // records of a tile row are contiguous).  The caller synchronises the CTA
 // before reusing `sm`.
-template <int ST, int R>
+template <int ST, int R, bool VAR = true>
 __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
                                                 LevelSmem<R, ST>& sm)
 {
@@ -341,13 +343,14 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
         sm.XL[k] = lum(c.x, c.y, c.z);
     }
     __syncthreads();
-    level_compute<ST, R>(a, lv, g, ra, rb, i0, j0, pre, sm);
+    level_compute<ST, R, VAR>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
-template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_level_tiled(FullArgs a, LevelGeom g)
+template <int ST, int R, bool VAR>
+__global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
     __shared__ LevelSmem<R, ST> sm;
-    full_level_tile<ST, R>(a, level_args_of(a), g, blockIdx.x, sm);
+    full_level_tile<ST, R, VAR>(a, level_args_of(a), g, blockIdx.x, sm);
 }
 
 // ------------------------------------------------------- TMA-staged level ----
@@ -379,7 +382,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase)
     }
 }
 
-template <int ST, int R>
+template <int ST, int R, bool VAR>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm)
 {
@@ -458,7 +461,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
         sm.XL[k] = lum(c.x, c.y, c.z);
     }
     __syncthreads();
-    level_compute<ST, R>(a, lv, g, ra, rb, i0, j0, pre, sm);
+    level_compute<ST, R, VAR>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
 // ------------------------------------------------------------- REF-EXACT ----

@@ -430,10 +430,9 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
         a.lout = res_layout(a.w, a.h, lv + 1);
         const LevelGeom g = level_geom(a.w, a.h, a.stride, kR);
         const dim3 lgrid(level_blocks(g)), lblk(kLvTX, kLvRows);
-        if (sv->f16)
-            k_full_level_tiled<ST_FP16, kR><<<lgrid, lblk, 0, st>>>(a, g);
-        else
-            k_full_level_tiled<ST_FP32, kR><<<lgrid, lblk, 0, st>>>(a, g);
+        auto k = sv->f16 ? (a.last ? k_full_level_tiled<ST_FP16, kR, false> : k_full_level_tiled<ST_FP16, kR, true>)
+                         : (a.last ? k_full_level_tiled<ST_FP32, kR, false> : k_full_level_tiled<ST_FP32, kR, true>);
+        k<<<lgrid, lblk, 0, st>>>(a, g);
         std::swap(src, oth);
     }
 }
