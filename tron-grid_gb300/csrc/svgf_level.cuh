@@ -203,6 +203,7 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
     float ar[R], ag[R], ab[R], aw[R], av[R];
     const float zs = a.sigma_z * float(s) * (1.0f / kLog2e);
     const float ez = kEpsZ * (1.0f / kLog2e);
+    const float kz_centre = rcp_approx(ez);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int c = (cj0 + k + 2) * T::SW + ci + 2;
@@ -223,14 +224,19 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
             sv = fmaf((q / 3 == 1 ? 0.5f : 0.25f) * (q % 3 == 1 ? 0.5f : 0.25f), pre.vn9[k][q], sv);
         const float gv = sv * rcp_approx(ky_sum * pre.kx_sum);
         kl[k] = kLog2e * rcp_approx(a.sigma_l * sqrt_approx(fmaxf(gv, 0.f)) + kEpsL);
-        const float A_ = zs * pre.gr[k].x, B_ = zs * pre.gr[k].y;
+        const float A_ = zs * pre.gr[k].x, B_ = zs * pre.gr[k].y, B2 = B_ + B_;
         // kz for the 13 offsets (dx, dy) with dy > 0 or (dy == 0 and dx >= 0);
-        // the other 12 offsets are their negations and share the value.
+        // the other 12 offsets are their negations and share the value.  The
+        // projections dx A + dy B are built from A, B and 2B (exact) with one
+        // operation each; offset (0, 0) has the constant 1 / eps.
+        kz[k][0] = kz_centre;
 #pragma unroll
-        for (int q = 0; q < 13; ++q) {
+        for (int q = 1; q < 13; ++q) {
             const int dx = (q < 3) ? q : ((q - 3) % 5) - 2;
             const int dy = (q < 3) ? 0 : 1 + (q - 3) / 5;
-            kz[k][q] = rcp_approx(fabsf(float(dx) * A_ + float(dy) * B_) + ez);
+            const float by = dy == 1 ? B_ : B2;
+            const float v = dy == 0 ? (dx == 1 ? A_ : A_ + A_) : (dx == 0 ? by : fmaf(float(dx), A_, by));
+            kz[k][q] = rcp_approx(fabsf(v) + ez);
         }
     }
 
