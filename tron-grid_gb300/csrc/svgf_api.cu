@@ -192,6 +192,22 @@ int validate_params(const tg_svgf_params& p)
 namespace tg {
 // Output rows per thread of the tiled a-trous kernels.
 constexpr int kLevelR = 2;
+
+typedef void (*LevelTmaFn)(FullArgs, LevelArgs, LevelGeom, const CUtensorMap, const CUtensorMap);
+typedef void (*LevelTiledFn)(FullArgs, LevelGeom);
+
+// The FULL a-trous kernel for a level: FP16 or FP32 records, VAR = false at the
+// last level (it writes only colour), PL at level 0 (staged from the planes).
+template <bool PL> LevelTmaFn level_tma_kernel(bool f16, bool last)
+{
+    if (f16) return last ? k_full_level_tma<ST_FP16, kLevelR, false, PL> : k_full_level_tma<ST_FP16, kLevelR, true, PL>;
+    return last ? k_full_level_tma<ST_FP32, kLevelR, false, PL> : k_full_level_tma<ST_FP32, kLevelR, true, PL>;
+}
+template <bool PL> LevelTiledFn level_tiled_kernel(bool f16, bool last)
+{
+    if (f16) return last ? k_full_level_tiled<ST_FP16, kLevelR, false, PL> : k_full_level_tiled<ST_FP16, kLevelR, true, PL>;
+    return last ? k_full_level_tiled<ST_FP32, kLevelR, false, PL> : k_full_level_tiled<ST_FP32, kLevelR, true, PL>;
+}
 enum Family { F_REF_INIT = 0, F_REF_LEVEL, F_FULL_TEMPORAL, F_FULL_VARIANCE, F_FULL_LEVEL, kFamilies };
 static const char* kFamilyName[kFamilies] = {"ref_init", "ref_level", "full_temporal", "full_variance", "full_level"};
 } // namespace tg
@@ -218,6 +234,8 @@ struct tg_svgf {
     int flags = 0;
     bool tma = false;                // a-trous tiles staged by TMA
     CUtensorMap tmaps[10];           // per level: the level's input records
+    bool tma0 = false;               // level 0 staged by TMA from the tc and guide planes
+    CUtensorMap tm_tc, tm_guide[2];  // row-major tc and guide[parity] (level 0 reads these, not records)
     // host-call staging: a ring of three sets, so that a frame's upload never
     // waits for the download of the frame two before it
     static constexpr int kStaging = 3;
@@ -352,6 +370,33 @@ void build_tensor_maps(tg_svgf* s)
         if (r != CUDA_SUCCESS) return;
     }
     s->tma = true;
+    // Level 0's planes: FP32 {4 floats, column, row}, FP16 {8-byte texel, column, row} (its row pitch must be a
+    // multiple of 16 bytes, so an odd width stages level 0 with plain loads).
+    s->tma0 = false;
+    void* planes[3] = {s->tc, s->guide[0], s->guide[1]};
+    CUtensorMap* maps[3] = {&s->tm_tc, &s->tm_guide[0], &s->tm_guide[1]};
+    for (int k = 0; k < 3; ++k) {
+        CUresult r;
+        if (f16) {
+            if ((8ull * s->w) % 16) return;
+            const cuuint64_t dim[2] = {s->w, s->h};
+            const cuuint64_t str[1] = {8ull * s->w};
+            const cuuint32_t box[2] = {LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH};
+            const cuuint32_t es[2] = {1, 1};
+            r = enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, planes[k], dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        } else {
+            const cuuint64_t dim[3] = {4, s->w, s->h};
+            const cuuint64_t str[2] = {16, 16ull * s->w};
+            const cuuint32_t box[3] = {4, LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH};
+            const cuuint32_t es[3] = {1, 1, 1};
+            r = enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, planes[k], dim, str, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        }
+        if (r != CUDA_SUCCESS) return;
+    }
+    s->tma0 = true;
 }
 
 void free_buffers(tg_svgf* s)
@@ -534,6 +579,7 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.fallback_frames = s->p.fallback_frames;
         a.col_dst = s->colA;
         a.var_off = col_var_offset_of(s->p, s->w, s->h);
+        a.planes0 = 1;  // level 0 reads tc, guide_cur and the variance plane; K1 and K2 write no records
         const double npx = double(s->w) * s->h;
         const double gb = f16 ? 8 : 16, c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
         const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +
@@ -542,8 +588,8 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         const double vb = f16 ? 2 : 4;    // variance plane entry
         const double rb = f16 ? 16 : 32;  // a-trous record
         // temporal: inputs + previous guide/history/moments, writes guide, tc, moments, depth gradient and
-        // the level-0 record + variance plane entry (every pixel with a history of fallback_frames or more)
-        launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm) + 8 + rb + vb), [&] {
+        // the variance plane entry (every pixel with a history of fallback_frames or more)
+        launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm) + 8 + vb), [&] {
             if (f16)
                 k_full_temporal<ST_FP16><<<grd, blk, 0, stream>>>(a);
             else
@@ -568,22 +614,22 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
             a.lin = res_layout(a.w, a.h, lv);
             a.lout = res_layout(a.w, a.h, lv + 1);
             // level: records (colour, variance, guide), variance plane and depth gradient in, records and
-            // variance plane (or the output) out; level 0 also reads the temporal colour's length and writes
-            // the history
-            const double lb = rb + vb + 8 + (a.last ? ob : rb + vb) + (lv == 0 ? 2 * c4 : 0);
+            // variance plane (or the output) out; level 0 reads tc (colour and length), guide and variance
+            // plane instead of records and also writes the history
+            const double lb = (lv == 0 ? c4 + gb : rb) + vb + 8 + (a.last ? ob : rb + vb) + (lv == 0 ? c4 : 0);
             const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
             const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
             // the last level writes only colour: its kernels leave out the variance propagation
             launch(s, stream, F_FULL_LEVEL, npx * lb, [&] {
-                if (s->tma) {
+                const bool pl = lv == 0;
+                if (s->tma && (!pl || s->tma0)) {
                     const LevelArgs la = level_args_of(a);
-                    auto k = f16 ? (a.last ? k_full_level_tma<ST_FP16, kLevelR, false> : k_full_level_tma<ST_FP16, kLevelR, true>)
-                                 : (a.last ? k_full_level_tma<ST_FP32, kLevelR, false> : k_full_level_tma<ST_FP32, kLevelR, true>);
-                    k<<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv]);
+                    if (pl)
+                        level_tma_kernel<true>(f16, a.last)<<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tm_tc, s->tm_guide[cur]);
+                    else
+                        level_tma_kernel<false>(f16, a.last)<<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv], s->tmaps[lv]);
                 } else {
-                    auto k = f16 ? (a.last ? k_full_level_tiled<ST_FP16, kLevelR, false> : k_full_level_tiled<ST_FP16, kLevelR, true>)
-                                 : (a.last ? k_full_level_tiled<ST_FP32, kLevelR, false> : k_full_level_tiled<ST_FP32, kLevelR, true>);
-                    k<<<lgrid, lblk, 0, stream>>>(a, lg);
+                    (pl ? level_tiled_kernel<true>(f16, a.last) : level_tiled_kernel<false>(f16, a.last))<<<lgrid, lblk, 0, stream>>>(a, lg);
                 }
             });
             void* t = src;

@@ -105,6 +105,10 @@ struct FullArgs {
     int sq_n; // squarings for sigma_n = 2^sq_n, -1 otherwise
     int max_history, fallback_frames;
     int level, stride, last;
+    // 1: level 0 stages its input from tc (colour), guide_cur (guide) and the
+    // variance plane, so K1 and K2 write only the variance plane entry of a
+    // pixel; 0: they also write its level-0 record
+    int planes0;
 };
 
 // K1: guide write, reprojection (bilinear 2x2 with depth/normal test), history
@@ -237,7 +241,7 @@ template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArg
     const float4 t = S::rt4(tcv);
     if (int(t.w) < a.fallback_frames) return true;
     const float v = S::rtm(mom).y;
-    S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, v), gv);
+    if (!a.planes0) S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, v), gv);
     S::st_var(a.col_dst, a.var_off, i, v);
     return false;
 }
@@ -311,8 +315,9 @@ __device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y
         var = fmaxf(0.0f, s2 / s0 - m1 * m1);
     }
     // level-0 input record: colour + variance, and the pixel's guide for the edge stops
-    S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var),
-              S::ld_graw(static_cast<const G*>(a.guide_cur), i));
+    if (!a.planes0)
+        S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var),
+                  S::ld_graw(static_cast<const G*>(a.guide_cur), i));
     S::st_var(a.col_dst, a.var_off, i, var);
 }
 

@@ -28,6 +28,8 @@
 
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "svgf_device.cuh"
 
 namespace tg {
@@ -311,10 +313,32 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
     }
 }
 
+// Level 0 read from the planes K1 writes instead of records (FullArgs::planes0):
+// the staged cell's colour from tc, its variance from the variance plane, its
+// guide from guide_cur (FP16: the octahedral code too).  The values are those
+// the level-0 record would hold.
+template <int ST>
+__device__ __forceinline__ void plane_cell(const FullArgs& a, const LevelArgs& lv, size_t j, float4& c, float4& n,
+                                           uint32_t& oct)
+{
+    typedef Stor<ST> S;
+    const float4 t = S::ld4(static_cast<const typename S::c4_t*>(a.tc), j);
+    c = make_float4(t.x, t.y, t.z, S::ld_var(lv.col_src, lv.var_off, j));
+    if constexpr (ST == ST_FP16) {
+        const uint2 u = S::ld_graw(static_cast<const typename S::guide_t*>(a.guide_cur), j);
+        const float3 v = oct16_decode_fast(u.x);
+        n = make_float4(v.x, v.y, v.z, __uint_as_float(u.y));
+        oct = u.x;
+    } else {
+        n = S::ld_graw(static_cast<const typename S::guide_t*>(a.guide_cur), j);
+        oct = 0;
+    }
+}
+
 // One tile of one level, staged with plain coalesced loads (the residue-major
-// records of a tile row are contiguous).  The caller synchronises the CTA
-// before reusing `sm`.
-template <int ST, int R, bool VAR = true>
+// records of a tile row are contiguous; PL: level 0 from the planes).  The
+// caller synchronises the CTA before reusing `sm`.
+template <int ST, int R, bool VAR = true, bool PL = false>
 __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
                                                 LevelSmem<R, ST>& sm)
 {
@@ -335,7 +359,9 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
         if (staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
             const int sj = k / T::SW, si = k - sj * T::SW;
             const size_t ri = plane + (j0 + sj - 2) * pw + (i0 + si - 2);
-            if constexpr (ST == ST_FP16) {
+            if constexpr (PL) {
+                plane_cell<ST>(a, lv, ri, c, n, oct);
+            } else if constexpr (ST == ST_FP16) {
                 const uint4 u = __ldg(src + ri);
                 S::decode_rec(u, c, n);
                 oct = u.z;
@@ -352,11 +378,11 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
     level_compute<ST, R, VAR>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
-template <int ST, int R, bool VAR>
+template <int ST, int R, bool VAR, bool PL = false>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
     __shared__ LevelSmem<R, ST> sm;
-    full_level_tile<ST, R, VAR>(a, level_args_of(a), g, blockIdx.x, sm);
+    full_level_tile<ST, R, VAR, PL>(a, level_args_of(a), g, blockIdx.x, sm);
 }
 
 // ------------------------------------------------------- TMA-staged level ----
@@ -388,12 +414,29 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase)
     }
 }
 
-template <int ST, int R, bool VAR>
+// Landing area of level 0's two FP16 plane boxes (8-byte tc and guide texels),
+// which cannot be decoded in place; other instantiations use an empty one.
+template <int R> struct __align__(128) PlaneRaw16 {
+    uint2 c[LevelTile<R>::N];
+    uint2 g[LevelTile<R>::N];
+};
+struct NoRaw {};
+
+// PL (level 0 with FullArgs::planes0): the box comes from two row-major images
+// instead of the records, tc through `tm` and guide_cur through `tm2` (FP32:
+// 3-D maps {4 floats, column, row} landing as X0 and X1; FP16: 2-D maps of
+// 8-byte texels landing in PlaneRaw16); each staged cell's variance comes from
+// the variance plane, loaded before the wait.
+template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
-    k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm)
+    k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm,
+                     const __grid_constant__ CUtensorMap tm2)
 {
     typedef LevelTile<R> T;
+    typedef typename std::conditional<PL && ST == ST_FP16, PlaneRaw16<R>, NoRaw>::type Raw16;
+    constexpr int kCells = (T::N + kLvTX * kLvRows - 1) / (kLvTX * kLvRows);
     __shared__ LevelSmem<R, ST> sm;
+    __shared__ Raw16 raw16;
     __shared__ __align__(8) uint64_t bar;
     // FP16 records (16 B) land in the X1 array and are decoded in place: each
     // thread reads raw record k before it writes X0/X1/XL entry k.
@@ -412,7 +455,28 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     const int plane = (rb << lv.lin.lg) + ra;
     if (tid == 0) {
         const uint64_t map = reinterpret_cast<uint64_t>(&tm);
-        if constexpr (ST == ST_FP32) {
+        if constexpr (PL) {
+            const uint64_t map2 = reinterpret_cast<uint64_t>(&tm2);
+            const uint32_t bytes = 2u * T::N * (ST == ST_FP16 ? 8u : 16u);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
+            if constexpr (ST == ST_FP16) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    asm volatile(
+                        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                        "[%4];" ::"r"(smem_u32(h == 0 ? raw16.c : raw16.g)),
+                        "l"(h == 0 ? map : map2), "r"(i0 - 2), "r"(j0 - 2), "r"(ubar)
+                        : "memory");
+            } else {
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    asm volatile(
+                        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                        "%4}], [%5];" ::"r"(smem_u32(h == 0 ? sm.X0 : sm.X1)),
+                        "l"(h == 0 ? map : map2), "r"(0), "r"(i0 - 2), "r"(j0 - 2), "r"(ubar)
+                        : "memory");
+            }
+        } else if constexpr (ST == ST_FP32) {
             const uint32_t bytes = 2u * T::N * 16u;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
 #pragma unroll
@@ -436,6 +500,19 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     }
     CentrePre<ST, R> pre;
     level_prefetch<ST, R>(a, lv, s, ra, rb, i0, j0, pre);
+    // PL: the staged cells' variances (the plane is row-major at level 0)
+    float cv[PL ? kCells : 1];
+    if constexpr (PL) {
+#pragma unroll
+        for (int e = 0; e < kCells; ++e) {
+            const int k = tid + e * kLvTX * kLvRows;
+            cv[e] = 0.f;
+            if (k < T::N && staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
+                const int sj = k / T::SW, si = k - sj * T::SW;
+                cv[e] = Stor<ST>::ld_var(lv.col_src, lv.var_off, size_t(j0 + sj - 2) * a.w + (i0 + si - 2));
+            }
+        }
+    }
     const bool landed = mbar_wait_bounded(ubar, 0);
     if (__syncthreads_or(!landed)) {
         if (tid == 0) {
@@ -445,25 +522,34 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
         return;
     }
     // Zero the cells outside the image, compute luminance (and decode FP16 records).
-    for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+#pragma unroll
+    for (int e = 0; e < kCells; ++e) {
+        const int k = tid + e * kLvTX * kLvRows;
+        if (k >= T::N) break;
         const bool in = staged_inside<R>(a, s, ra, rb, i0, j0, k);
         float4 c, n;
-        if constexpr (ST == ST_FP16) {
+        if constexpr (PL && ST == ST_FP16) {
+            const float4 t = unpack_h4(raw16.c[k]);
+            const uint2 u = raw16.g[k];
+            const float3 v = oct16_decode_fast(u.x);
+            c = make_float4(t.x, t.y, t.z, cv[e]);
+            n = make_float4(v.x, v.y, v.z, __uint_as_float(u.y));
+            sm.XO[k] = u.x;
+        } else if constexpr (ST == ST_FP16) {
             const uint4 u = raw[k];
             Stor<ST_FP16>::decode_rec(u, c, n);
             sm.XO[k] = u.z;
         } else {
             c = sm.X0[k];
             n = sm.X1[k];
+            if constexpr (PL) c.w = cv[e];
         }
         if (!in) {
             c = make_float4(0.f, 0.f, 0.f, 0.f);
             n = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        if (ST == ST_FP16 || !in) {
-            sm.X0[k] = c;
-            sm.X1[k] = n;
-        }
+        if (ST == ST_FP16 || PL || !in) sm.X0[k] = c;
+        if (ST == ST_FP16 || !in) sm.X1[k] = n;
         sm.XL[k] = lum(c.x, c.y, c.z);
     }
     __syncthreads();
