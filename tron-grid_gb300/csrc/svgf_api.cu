@@ -335,9 +335,10 @@ EncodeTiledFn encode_tiled()
     return fn;
 }
 
-// One tensor map per a-trous level over that level's input records in the
-// residue-major layout of stride 2^L: FP32 {4 floats, record half, column, row,
-// plane}, FP16 {4 words, column, row, plane}; box = one 36 x 20 halo tile.
+// One tensor map per a-trous level L >= 1 over that level's input records in
+// the residue-major layout of stride 2^L: FP32 {4 floats, record half, column,
+// row, plane}, FP16 {4 words, column, row, plane}; box = one 36 x 20 halo tile.
+// Level 0 has no records: its maps cover the tc and guide planes.
 void build_tensor_maps(tg_svgf* s)
 {
     s->tma = false;
@@ -345,7 +346,7 @@ void build_tensor_maps(tg_svgf* s)
     EncodeTiledFn enc = encode_tiled();
     if (!enc) return;
     const bool f16 = s->p.storage == TG_SVGF_STORAGE_FP16;
-    for (int lv = 0; lv < s->p.levels; ++lv) {
+    for (int lv = 1; lv < s->p.levels; ++lv) {
         const ResLayout L = res_layout(int(s->w), int(s->h), lv);
         void* base = (lv & 1) ? s->colB : s->colA;
         const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
@@ -579,7 +580,6 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.fallback_frames = s->p.fallback_frames;
         a.col_dst = s->colA;
         a.var_off = col_var_offset_of(s->p, s->w, s->h);
-        a.planes0 = 1;  // level 0 reads tc, guide_cur and the variance plane; K1 and K2 write no records
         const double npx = double(s->w) * s->h;
         const double gb = f16 ? 8 : 16, c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
         const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +

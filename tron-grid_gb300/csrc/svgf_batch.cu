@@ -134,10 +134,17 @@ PixFn pixel_kernel(bool f16, int stage)
     return stage == 0 ? k_ms_pixel<ST_FP32, 0> : k_ms_pixel<ST_FP32, 1>;
 }
 
-LevFn level_kernel(bool f16, int R)
+template <int ST, int R> LevFn level_kernel_r(int L, int levels)
 {
-    if (f16) return R == 1 ? k_ms_level<ST_FP16, 1> : k_ms_level<ST_FP16, 2>;
-    return R == 1 ? k_ms_level<ST_FP32, 1> : k_ms_level<ST_FP32, 2>;
+    if (L == 0) return k_ms_level<ST, R, true, true>;
+    return L == levels - 1 ? k_ms_level<ST, R, false, false> : k_ms_level<ST, R, true, false>;
+}
+
+// The stage kernel of level L: level 0 stages from the planes, the last level writes only colour.
+LevFn level_kernel(bool f16, int R, int L, int levels)
+{
+    if (f16) return R == 1 ? level_kernel_r<ST_FP16, 1>(L, levels) : level_kernel_r<ST_FP16, 2>(L, levels);
+    return R == 1 ? level_kernel_r<ST_FP32, 1>(L, levels) : level_kernel_r<ST_FP32, 2>(L, levels);
 }
 
 // One launch per stage over the work table of buffer k.
@@ -153,7 +160,8 @@ cudaError_t launch_stages(tg_svgf_batch* b, int k, cudaStream_t s)
         if (st < 2)
             pixel_kernel(f16, int(st))<<<g[st], dim3(kBlockX, kBlockY), 0, s>>>(b->d_table[k], b->cap);
         else
-            level_kernel(f16, b->R)<<<g[st], dim3(kLvTX, kLvRows), 0, s>>>(b->d_table[k], b->cap, int(st) - 2);
+            level_kernel(f16, b->R, int(st) - 2, b->p.levels)<<<g[st], dim3(kLvTX, kLvRows), 0, s>>>(b->d_table[k], b->cap,
+                                                                                                    int(st) - 2);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -159,7 +159,13 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
                 lv.lin = res_layout(a.w, a.h, L);
                 lv.lout = res_layout(a.w, a.h, L + 1);
                 const LevelGeom g = level_geom(a.w, a.h, 1 << L, R);
-                full_level_tile<ST, R>(a, lv, g, local, sm);
+                // level 0 stages from the planes; the last level writes only colour
+                if (L == 0)
+                    full_level_tile<ST, R, true, true>(a, lv, g, local, sm);
+                else if (lv.last)
+                    full_level_tile<ST, R, false, false>(a, lv, g, local, sm);
+                else
+                    full_level_tile<ST, R, true, false>(a, lv, g, local, sm);
                 __syncthreads();
             }
         }
@@ -211,7 +217,8 @@ __global__ void __launch_bounds__(kBlockX* kBlockY) k_ms_pixel(const char* __res
     }
 }
 
-template <int ST, int R>
+// VAR = false at the last level (colour only); PL at level 0 (staged from the planes).
+template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level(const char* __restrict__ table, int cap, int L)
 {
     __shared__ LevelSmem<R, ST> sm;
@@ -230,7 +237,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level
     lv.last = L == hd->levels - 1;
     lv.lin = res_layout(a.w, a.h, L);
     lv.lout = res_layout(a.w, a.h, L + 1);
-    full_level_tile<ST, R>(a, lv, level_geom(a.w, a.h, 1 << L, R), item - pf[j], sm);
+    full_level_tile<ST, R, VAR, PL>(a, lv, level_geom(a.w, a.h, 1 << L, R), item - pf[j], sm);
 }
 
 } // namespace tg

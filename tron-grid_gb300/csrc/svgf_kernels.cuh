@@ -105,17 +105,14 @@ struct FullArgs {
     int sq_n; // squarings for sigma_n = 2^sq_n, -1 otherwise
     int max_history, fallback_frames;
     int level, stride, last;
-    // 1: level 0 stages its input from tc (colour), guide_cur (guide) and the
-    // variance plane, so K1 and K2 write only the variance plane entry of a
-    // pixel; 0: they also write its level-0 record
-    int planes0;
 };
 
 // K1: guide write, reprojection (bilinear 2x2 with depth/normal test), history
 // length, colour EMA and mean-centred moment EMA.  A pixel whose history is at
-// least `fallback_frames` long also gets its level-0 record (colour, temporal
-// variance, guide) here, from the values as stored; the function returns true
-// for the others, whose variance needs the neighbours' moments (K2).
+// least `fallback_frames` long also gets its level-0 variance-plane entry (the
+// temporal variance as stored) here; the function returns true for the
+// others, whose variance needs the neighbours' moments (K2).  Level 0 stages
+// its input from tc, guide_cur and that plane, so no level-0 record is written.
 template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArgs& a, int x, int y)
 {
     typedef Stor<ST> S;
@@ -240,16 +237,14 @@ template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArg
     S::stm(static_cast<M*>(a.mom_cur), i, mom);
     const float4 t = S::rt4(tcv);
     if (int(t.w) < a.fallback_frames) return true;
-    const float v = S::rtm(mom).y;
-    if (!a.planes0) S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, v), gv);
-    S::st_var(a.col_dst, a.var_off, i, v);
+    S::st_var(a.col_dst, a.var_off, i, S::rtm(mom).y);
     return false;
 }
 
 // K2: for histories shorter than `fallback_frames`, the variance is a 7x7
 // depth/normal-weighted spatial estimate from the neighbours' moments; writes
-// the level-0 record (colour, variance, guide) of such a pixel.  The other
-// pixels' records come from K1.
+// the level-0 variance-plane entry of such a pixel.  The other pixels' entries
+// come from K1.
 //
 // A CTA stages the guides (decoded) and moments of its pixel block plus a
 // 3-pixel halo in shared memory.  Cells outside the image hold a zero normal,
@@ -267,7 +262,6 @@ template <int ST>
 __device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y, int cell, const VarTile& vt)
 {
     typedef Stor<ST> S;
-    typedef typename S::guide_t G;
     typedef typename S::c4_t C4;
     const size_t i = size_t(y) * a.w + x;
     const float4 t = S::ld4(static_cast<const C4*>(a.tc), i);
@@ -314,10 +308,6 @@ __device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y
         const float m1 = s1 / s0;
         var = fmaxf(0.0f, s2 / s0 - m1 * m1);
     }
-    // level-0 input record: colour + variance, and the pixel's guide for the edge stops
-    if (!a.planes0)
-        S::st_rec(static_cast<typename S::rec_t*>(a.col_dst), i, make_float4(t.x, t.y, t.z, var),
-                  S::ld_graw(static_cast<const G*>(a.guide_cur), i));
     S::st_var(a.col_dst, a.var_off, i, var);
 }
 

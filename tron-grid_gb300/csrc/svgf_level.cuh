@@ -313,10 +313,10 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
     }
 }
 
-// Level 0 read from the planes K1 writes instead of records (FullArgs::planes0):
-// the staged cell's colour from tc, its variance from the variance plane, its
-// guide from guide_cur (FP16: the octahedral code too).  The values are those
-// the level-0 record would hold.
+// Level 0 reads the planes K1 writes instead of records: the staged cell's
+// colour from tc, its variance from the variance plane, its guide from
+// guide_cur (FP16: the octahedral code too).  Every FULL path stages level 0
+// this way (PL); K1 and K2 write no level-0 records.
 template <int ST>
 __device__ __forceinline__ void plane_cell(const FullArgs& a, const LevelArgs& lv, size_t j, float4& c, float4& n,
                                            uint32_t& oct)
@@ -422,7 +422,7 @@ template <int R> struct __align__(128) PlaneRaw16 {
 };
 struct NoRaw {};
 
-// PL (level 0 with FullArgs::planes0): the box comes from two row-major images
+// PL (level 0): the box comes from two row-major images
 // instead of the records, tc through `tm` and guide_cur through `tm2` (FP32:
 // 3-D maps {4 floats, column, row} landing as X0 and X1; FP16: 2-D maps of
 // 8-byte texels landing in PlaneRaw16); each staged cell's variance comes from

@@ -339,10 +339,15 @@ void launch_stage_kernels(tg_svgf_server* sv, int k, const std::vector<int>& gri
             else
                 (g == 0 ? k_ms_pixel<ST_FP32, 0> : k_ms_pixel<ST_FP32, 1>)<<<grids[g], dim3(kBlockX, kBlockY), 0, st>>>(
                     sv->d_table[k], sv->cap);
-        } else if (sv->f16) {
-            k_ms_level<ST_FP16, kR><<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, int(g) - 2);
         } else {
-            k_ms_level<ST_FP32, kR><<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, int(g) - 2);
+            // level 0 stages from the planes, the last level writes only colour
+            const int L = int(g) - 2;
+            const bool pl = L == 0, var = pl || L != sv->d.params.levels - 1;
+            auto k16 = pl ? k_ms_level<ST_FP16, kR, true, true>
+                          : (var ? k_ms_level<ST_FP16, kR, true, false> : k_ms_level<ST_FP16, kR, false, false>);
+            auto k32 = pl ? k_ms_level<ST_FP32, kR, true, true>
+                          : (var ? k_ms_level<ST_FP32, kR, true, false> : k_ms_level<ST_FP32, kR, false, false>);
+            (sv->f16 ? k16 : k32)<<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, L);
         }
     }
 }
@@ -430,9 +435,12 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
         a.lout = res_layout(a.w, a.h, lv + 1);
         const LevelGeom g = level_geom(a.w, a.h, a.stride, kR);
         const dim3 lgrid(level_blocks(g)), lblk(kLvTX, kLvRows);
-        auto k = sv->f16 ? (a.last ? k_full_level_tiled<ST_FP16, kR, false> : k_full_level_tiled<ST_FP16, kR, true>)
-                         : (a.last ? k_full_level_tiled<ST_FP32, kR, false> : k_full_level_tiled<ST_FP32, kR, true>);
-        k<<<lgrid, lblk, 0, st>>>(a, g);
+        // level 0 stages from the planes, the last level writes only colour
+        auto k16 = lv == 0 ? k_full_level_tiled<ST_FP16, kR, true, true>
+                           : (a.last ? k_full_level_tiled<ST_FP16, kR, false> : k_full_level_tiled<ST_FP16, kR, true>);
+        auto k32 = lv == 0 ? k_full_level_tiled<ST_FP32, kR, true, true>
+                           : (a.last ? k_full_level_tiled<ST_FP32, kR, false> : k_full_level_tiled<ST_FP32, kR, true>);
+        (sv->f16 ? k16 : k32)<<<lgrid, lblk, 0, st>>>(a, g);
         std::swap(src, oth);
     }
 }
