@@ -337,7 +337,8 @@ EncodeTiledFn encode_tiled()
 
 // One tensor map per a-trous level L >= 1 over that level's input records in
 // the residue-major layout of stride 2^L: FP32 {4 floats, record half, column,
-// row, plane}, FP16 {4 words, column, row, plane}; box = one 36 x 20 halo tile.
+// row, plane}, FP16 {8-byte element (two per record), row, plane}; box = one
+// 36 x 20 halo tile.
 // Level 0 has no records: its maps cover the tc and guide planes.
 void build_tensor_maps(tg_svgf* s)
 {
@@ -352,11 +353,12 @@ void build_tensor_maps(tg_svgf* s)
         const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
         CUresult r;
         if (f16) {
-            const cuuint64_t dim[4] = {4, cuuint64_t(L.pw), cuuint64_t(L.ph), planes};
-            const cuuint64_t str[3] = {16, 16ull * L.pw, 16ull * L.pw * L.ph};
-            const cuuint32_t box[4] = {4, LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1};
-            const cuuint32_t es[4] = {1, 1, 1, 1};
-            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, base, dim, str, box, es,
+            // a row of 16-byte records as 2 pw 8-byte elements: one contiguous 576-byte line per tile row
+            const cuuint64_t dim[3] = {2ull * L.pw, cuuint64_t(L.ph), planes};
+            const cuuint64_t str[2] = {16ull * L.pw, 16ull * L.pw * L.ph};
+            const cuuint32_t box[3] = {2 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1};
+            const cuuint32_t es[3] = {1, 1, 1};
+            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, dim, str, box, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         } else {

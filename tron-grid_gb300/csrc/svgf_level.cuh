@@ -391,7 +391,8 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_lev
 // one elected thread issues cp.async.bulk.tensor for the tile's box of
 // residue-major records (5-D map {4 floats, record half, column, row, plane}
 // for FP32, so that the box of each record half lands as one dense float4
-// array; 4-D map {4 words, column, row, plane} for FP16), completion is
+// array; for FP16 a 3-D map {8-byte element, row, plane}, so that each tile row
+// of 16-byte records is one contiguous 576-byte line), completion is
 // tracked by an mbarrier transaction count, and cells outside the plane array
 // arrive zero-filled.  The wait is bounded: a box that has not landed after
 // about a second sets a->err and the CTA returns.
@@ -489,12 +490,13 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
                     : "memory");
             }
         } else {
+            // rows of 8-byte elements, two per record: x = 2 (i0 - 2) is even, so the box starts on 16 bytes
             const uint32_t bytes = T::N * 16u;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
             asm volatile(
-                "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-                "[%6];" ::"r"(smem_u32(raw)),
-                "l"(map), "r"(0), "r"(i0 - 2), "r"(j0 - 2), "r"(plane), "r"(ubar)
+                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+                "[%5];" ::"r"(smem_u32(raw)),
+                "l"(map), "r"(2 * (i0 - 2)), "r"(j0 - 2), "r"(plane), "r"(ubar)
                 : "memory");
         }
     }
