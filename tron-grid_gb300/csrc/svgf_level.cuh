@@ -135,7 +135,9 @@ template <int ST, int R> struct CentrePre {
     float kx_sum;
 };
 
-template <int ST, int R>
+// IN: the CTA's tile, its halo and every centre's 3x3 neighbourhood lie inside
+// the image (tile_interior), so no access needs a bounds test.
+template <int ST, int R, bool IN>
 __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArgs& lv, int s, int ra, int rb, int i0,
                                                int j0, CentrePre<ST, R>& pre)
 {
@@ -147,10 +149,10 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
         const int qx = cx + e - 1;
-        cxv[e] = unsigned(qx) < unsigned(a.w);
+        cxv[e] = IN || unsigned(qx) < unsigned(a.w);
         cxo[e] = (qx & m) * P + (qx >> lg);
     }
-    pre.kx_sum = (cxv[0] ? 0.25f : 0.f) + (cxv[1] ? 0.5f : 0.f) + (cxv[2] ? 0.25f : 0.f);
+    pre.kx_sum = IN ? 1.f : (cxv[0] ? 0.25f : 0.f) + (cxv[1] ? 0.5f : 0.f) + (cxv[2] ? 0.25f : 0.f);
     // Every output row y = rb + s jj of this thread has residue rb, so neighbour row y + f - 1 lies in plane row
     // (rb + f - 1) mod s at position jj + floor((rb + f - 1) / s): its offset is a per-thread constant plus jj pw.
     const int j_base = (j0 + int(threadIdx.y) * R) * pw;
@@ -164,11 +166,11 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int y = rb + s * (j0 + int(threadIdx.y) * R + k);
-        pre.valid[k] = cx < a.w && y < a.h;
+        pre.valid[k] = IN || (cx < a.w && y < a.h);
         pre.gr[k] = pre.valid[k] ? a.grad[y * a.w + cx] : make_float2(0.f, 0.f);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-            const bool oy = pre.valid[k] && unsigned(y + f - 1) < unsigned(a.h);
+            const bool oy = pre.valid[k] && (IN || unsigned(y + f - 1) < unsigned(a.h));
 #pragma unroll
             for (int e = 0; e < 3; ++e)
                 pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::var_at(vp, rowf[f] + k * pw + cxo[e]) : 0.f;
@@ -187,10 +189,19 @@ __device__ __forceinline__ bool staged_inside(const FullArgs& a, int s, int ra, 
     return j >= 0 && i >= 0 && rb + s * j < a.h && ra + s * i < a.w;
 }
 
+// Whether the tile at (i0, j0) of residue (ra, rb), with its 2-cell halo, lies
+// inside the image; then so do its centres and their 3x3 neighbourhoods.
+template <int R>
+__device__ __forceinline__ bool tile_interior(const FullArgs& a, int s, int ra, int rb, int i0, int j0)
+{
+    typedef LevelTile<R> T;
+    return i0 >= 2 && j0 >= 2 && ra + s * (i0 + T::TX + 1) < a.w && rb + s * (j0 + T::TY + 1) < a.h;
+}
+
 // Everything after staging: per-centre set-up, the taps, the output records.
 // VAR = false leaves out the variance propagation (sum of w^2 var): the last
 // level writes only colour.
-template <int ST, int R, bool VAR = true>
+template <int ST, int R, bool VAR, bool IN>
 __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra,
                                               int rb, int i0, int j0, const CentrePre<ST, R>& pre,
                                               const LevelSmem<R, ST>& sm)
@@ -224,7 +235,9 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
 #pragma unroll
         for (int q = 0; q < 9; ++q)
             sv = fmaf((q / 3 == 1 ? 0.5f : 0.25f) * (q % 3 == 1 ? 0.5f : 0.25f), pre.vn9[k][q], sv);
-        const float gv = sv * rcp_approx(ky_sum * pre.kx_sum);
+        // (an inside pixel's weights sum to 1: its blur is sv itself on either path)
+        const float kk = ky_sum * pre.kx_sum;
+        const float gv = (IN || kk == 1.0f) ? sv : sv * rcp_approx(kk);
         kl[k] = kLog2e * rcp_approx(a.sigma_l * sqrt_approx(fmaxf(gv, 0.f)) + kEpsL);
         const float A_ = zs * pre.gr[k].x, B_ = zs * pre.gr[k].y, B2 = B_ + B_;
         // kz for the 13 offsets (dx, dy) with dy > 0 or (dy == 0 and dx >= 0);
@@ -338,25 +351,23 @@ __device__ __forceinline__ void plane_cell(const FullArgs& a, const LevelArgs& l
 // One tile of one level, staged with plain coalesced loads (the residue-major
 // records of a tile row are contiguous; PL: level 0 from the planes).  The
 // caller synchronises the CTA before reusing `sm`.
-template <int ST, int R, bool VAR = true, bool PL = false>
-__device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
-                                                LevelSmem<R, ST>& sm)
+template <int ST, int R, bool VAR, bool PL, bool IN>
+__device__ __forceinline__ void level_tile_body(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra,
+                                                int rb, int i0, int j0, LevelSmem<R, ST>& sm)
 {
     typedef Stor<ST> S;
     typedef typename S::rec_t RT;
     typedef LevelTile<R> T;
-    int ra, rb, i0, j0;
-    level_block(g, bid, T::TX, T::TY, ra, rb, i0, j0);
     const int s = g.s;
     CentrePre<ST, R> pre;
-    level_prefetch<ST, R>(a, lv, s, ra, rb, i0, j0, pre);
+    level_prefetch<ST, R, IN>(a, lv, s, ra, rb, i0, j0, pre);
     const RT* src = static_cast<const RT*>(lv.col_src);
     const int pw = lv.lin.pw, P = lv.lin.pw * lv.lin.ph;
     const int plane = ((rb << lv.lin.lg) + ra) * P;
     for (int k = threadIdx.y * kLvTX + threadIdx.x; k < T::N; k += kLvTX * kLvRows) {
         float4 c = make_float4(0.f, 0.f, 0.f, 0.f), n = make_float4(0.f, 0.f, 0.f, 0.f);
         uint32_t oct = 0;
-        if (staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
+        if (IN || staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
             const int sj = k / T::SW, si = k - sj * T::SW;
             const size_t ri = plane + (j0 + sj - 2) * pw + (i0 + si - 2);
             if constexpr (PL) {
@@ -375,7 +386,19 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
         sm.XL[k] = lum(c.x, c.y, c.z);
     }
     __syncthreads();
-    level_compute<ST, R, VAR>(a, lv, g, ra, rb, i0, j0, pre, sm);
+    level_compute<ST, R, VAR, IN>(a, lv, g, ra, rb, i0, j0, pre, sm);
+}
+
+template <int ST, int R, bool VAR = true, bool PL = false>
+__device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
+                                                LevelSmem<R, ST>& sm)
+{
+    int ra, rb, i0, j0;
+    level_block(g, bid, LevelTile<R>::TX, LevelTile<R>::TY, ra, rb, i0, j0);
+    if (tile_interior<R>(a, g.s, ra, rb, i0, j0))
+        level_tile_body<ST, R, VAR, PL, true>(a, lv, g, ra, rb, i0, j0, sm);
+    else
+        level_tile_body<ST, R, VAR, PL, false>(a, lv, g, ra, rb, i0, j0, sm);
 }
 
 template <int ST, int R, bool VAR, bool PL = false>
@@ -428,6 +451,75 @@ struct NoRaw {};
 // 3-D maps {4 floats, column, row} landing as X0 and X1; FP16: 2-D maps of
 // 8-byte texels landing in PlaneRaw16); each staged cell's variance comes from
 // the variance plane, loaded before the wait.
+// The TMA kernel after its copy is issued: prefetch, bounded wait, fix-up,
+// compute.  IN: the tile is interior (tile_interior), so no cell needs a test.
+template <int ST, int R, bool VAR, bool PL, bool IN, class Raw16>
+__device__ __forceinline__ void tma_tile_body(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra, int rb,
+                                              int i0, int j0, int tid, uint32_t ubar, LevelSmem<R, ST>& sm,
+                                              const Raw16& raw16)
+{
+    typedef LevelTile<R> T;
+    constexpr int kCells = (T::N + kLvTX * kLvRows - 1) / (kLvTX * kLvRows);
+    const int s = g.s;
+    const uint4* raw = reinterpret_cast<const uint4*>(sm.X1);
+    CentrePre<ST, R> pre;
+    level_prefetch<ST, R, IN>(a, lv, s, ra, rb, i0, j0, pre);
+    // PL: the staged cells' variances (the plane is row-major at level 0)
+    float cv[PL ? kCells : 1];
+    if constexpr (PL) {
+#pragma unroll
+        for (int e = 0; e < kCells; ++e) {
+            const int k = tid + e * kLvTX * kLvRows;
+            cv[e] = 0.f;
+            if (k < T::N && (IN || staged_inside<R>(a, s, ra, rb, i0, j0, k))) {
+                const int sj = k / T::SW, si = k - sj * T::SW;
+                cv[e] = Stor<ST>::ld_var(lv.col_src, lv.var_off, size_t(j0 + sj - 2) * a.w + (i0 + si - 2));
+            }
+        }
+    }
+    const bool landed = mbar_wait_bounded(ubar, 0);
+    if (__syncthreads_or(!landed)) {
+        if (tid == 0) {
+            if (a.err) atomicExch(a.err, 1);
+            mbar_wait_bounded(ubar, 0);  // give the copy a second bounded chance to retire
+        }
+        return;
+    }
+    // Zero the cells outside the image, compute luminance (and decode FP16 records).
+#pragma unroll
+    for (int e = 0; e < kCells; ++e) {
+        const int k = tid + e * kLvTX * kLvRows;
+        if (k >= T::N) break;
+        const bool in = IN || staged_inside<R>(a, s, ra, rb, i0, j0, k);
+        float4 c, n;
+        if constexpr (PL && ST == ST_FP16) {
+            const float4 t = unpack_h4(raw16.c[k]);
+            const uint2 u = raw16.g[k];
+            const float3 v = oct16_decode_fast(u.x);
+            c = make_float4(t.x, t.y, t.z, cv[e]);
+            n = make_float4(v.x, v.y, v.z, __uint_as_float(u.y));
+            sm.XO[k] = u.x;
+        } else if constexpr (ST == ST_FP16) {
+            const uint4 u = raw[k];
+            Stor<ST_FP16>::decode_rec(u, c, n);
+            sm.XO[k] = u.z;
+        } else {
+            c = sm.X0[k];
+            n = sm.X1[k];
+            if constexpr (PL) c.w = cv[e];
+        }
+        if (!in) {
+            c = make_float4(0.f, 0.f, 0.f, 0.f);
+            n = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        if (ST == ST_FP16 || PL || !in) sm.X0[k] = c;
+        if (ST == ST_FP16 || !in) sm.X1[k] = n;
+        sm.XL[k] = lum(c.x, c.y, c.z);
+    }
+    __syncthreads();
+    level_compute<ST, R, VAR, IN>(a, lv, g, ra, rb, i0, j0, pre, sm);
+}
+
 template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm,
@@ -435,7 +527,6 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
 {
     typedef LevelTile<R> T;
     typedef typename std::conditional<PL && ST == ST_FP16, PlaneRaw16<R>, NoRaw>::type Raw16;
-    constexpr int kCells = (T::N + kLvTX * kLvRows - 1) / (kLvTX * kLvRows);
     __shared__ LevelSmem<R, ST> sm;
     __shared__ Raw16 raw16;
     __shared__ __align__(8) uint64_t bar;
@@ -500,62 +591,10 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
                 : "memory");
         }
     }
-    CentrePre<ST, R> pre;
-    level_prefetch<ST, R>(a, lv, s, ra, rb, i0, j0, pre);
-    // PL: the staged cells' variances (the plane is row-major at level 0)
-    float cv[PL ? kCells : 1];
-    if constexpr (PL) {
-#pragma unroll
-        for (int e = 0; e < kCells; ++e) {
-            const int k = tid + e * kLvTX * kLvRows;
-            cv[e] = 0.f;
-            if (k < T::N && staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
-                const int sj = k / T::SW, si = k - sj * T::SW;
-                cv[e] = Stor<ST>::ld_var(lv.col_src, lv.var_off, size_t(j0 + sj - 2) * a.w + (i0 + si - 2));
-            }
-        }
-    }
-    const bool landed = mbar_wait_bounded(ubar, 0);
-    if (__syncthreads_or(!landed)) {
-        if (tid == 0) {
-            if (a.err) atomicExch(a.err, 1);
-            mbar_wait_bounded(ubar, 0);  // give the copy a second bounded chance to retire
-        }
-        return;
-    }
-    // Zero the cells outside the image, compute luminance (and decode FP16 records).
-#pragma unroll
-    for (int e = 0; e < kCells; ++e) {
-        const int k = tid + e * kLvTX * kLvRows;
-        if (k >= T::N) break;
-        const bool in = staged_inside<R>(a, s, ra, rb, i0, j0, k);
-        float4 c, n;
-        if constexpr (PL && ST == ST_FP16) {
-            const float4 t = unpack_h4(raw16.c[k]);
-            const uint2 u = raw16.g[k];
-            const float3 v = oct16_decode_fast(u.x);
-            c = make_float4(t.x, t.y, t.z, cv[e]);
-            n = make_float4(v.x, v.y, v.z, __uint_as_float(u.y));
-            sm.XO[k] = u.x;
-        } else if constexpr (ST == ST_FP16) {
-            const uint4 u = raw[k];
-            Stor<ST_FP16>::decode_rec(u, c, n);
-            sm.XO[k] = u.z;
-        } else {
-            c = sm.X0[k];
-            n = sm.X1[k];
-            if constexpr (PL) c.w = cv[e];
-        }
-        if (!in) {
-            c = make_float4(0.f, 0.f, 0.f, 0.f);
-            n = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        if (ST == ST_FP16 || PL || !in) sm.X0[k] = c;
-        if (ST == ST_FP16 || !in) sm.X1[k] = n;
-        sm.XL[k] = lum(c.x, c.y, c.z);
-    }
-    __syncthreads();
-    level_compute<ST, R, VAR>(a, lv, g, ra, rb, i0, j0, pre, sm);
+    if (tile_interior<R>(a, s, ra, rb, i0, j0))
+        tma_tile_body<ST, R, VAR, PL, true>(a, lv, g, ra, rb, i0, j0, tid, ubar, sm, raw16);
+    else
+        tma_tile_body<ST, R, VAR, PL, false>(a, lv, g, ra, rb, i0, j0, tid, ubar, sm, raw16);
 }
 
 // ------------------------------------------------------------- REF-EXACT ----
