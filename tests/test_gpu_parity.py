@@ -30,12 +30,13 @@ def _frames(spec, n):
     return [sc.frame(t) for t in range(n)]
 
 
-def _run_full_pair(dev, spec, n_frames, storage=tg.STORAGE_FP32, fp16_inputs=False, check=None):
+def _run_full_pair(dev, spec, n_frames, storage=tg.STORAGE_FP32, fp16_inputs=False, check=None, params=None):
     W, H = spec.width, spec.height
-    den = tg.Denoiser(W, H, mode=tg.MODE_FULL, storage=storage)
+    params = params or {}
+    den = tg.Denoiser(W, H, mode=tg.MODE_FULL, storage=storage, **params)
     st32 = oracle.FullState(H, W, np.float32)
     st64 = oracle.FullState(H, W, np.float64)
-    P = oracle.full_params()
+    P = oracle.full_params(**params)
     f16 = storage == tg.STORAGE_FP16
     out_dt = torch.float16 if f16 else torch.float32
     results = []
@@ -89,21 +90,37 @@ def test_full_fp32_odd_sizes(cuda_dev, wh):
     _run_full_pair(cuda_dev, spec, 5, check=_check_fp32)
 
 
+def _check_fp16(t, g, r32, r64):
+    e = rel_err(g, r32)
+    assert np.all(np.isfinite(g))
+    assert e.max() <= 2.0 ** -8, f"frame {t}: max rel {e.max():.3e} vs emulating oracle"
+    assert e.mean() <= 1e-5, f"frame {t}: mean rel {e.mean():.3e} vs emulating oracle"
+    l2 = rel_l2(g, r64)
+    assert l2 <= 1e-3, f"frame {t}: rel L2 vs float64 oracle {l2:.3e}"
+
+
 def test_full_fp16_storage(cuda_dev):
     """FP16 colour/moments, octahedral normals; FP16 radiance + OCT16 normal inputs."""
-    stats = []
-
-    def chk(t, g, r32, r64):
-        e = rel_err(g, r32)
-        assert np.all(np.isfinite(g))
-        assert e.max() <= 2.0 ** -8, f"frame {t}: max rel {e.max():.3e} vs emulating oracle"
-        assert e.mean() <= 1e-5, f"frame {t}: mean rel {e.mean():.3e} vs emulating oracle"
-        l2 = rel_l2(g, r64)
-        stats.append(l2)
-        assert l2 <= 1e-3, f"frame {t}: rel L2 vs float64 oracle {l2:.3e}"
-
     _run_full_pair(cuda_dev, scene.config1(320, 180, seed=4), 33, storage=tg.STORAGE_FP16, fp16_inputs=True,
-                   check=chk)
+                   check=_check_fp16)
+
+
+# Non-default parameters: every edge-stop width, both EMA weights, a shorter history cap and fallback window.
+ODD_PARAMS = dict(sigma_l=2.5, sigma_n=64.0, sigma_z=0.5, alpha=0.1, moments_alpha=0.3, max_history=16,
+                  fallback_frames=3)
+
+
+@pytest.mark.parametrize("levels", [1, 2, 3, 4])
+def test_full_fp32_level_counts_and_params(cuda_dev, levels):
+    """Fewer a-trous levels (with one level, level 0 is also the last: staged from the planes, colour only)."""
+    _run_full_pair(cuda_dev, scene.config1(96, 64, seed=5), 6, check=_check_fp32, params=dict(ODD_PARAMS, levels=levels))
+
+
+@pytest.mark.parametrize("W", [96, 97])
+def test_full_fp16_single_level(cuda_dev, W):
+    """One FP16 level at an even width (level 0 by TMA from the planes) and an odd one (plain loads)."""
+    _run_full_pair(cuda_dev, scene.config1(W, 64, seed=6), 6, storage=tg.STORAGE_FP16, fp16_inputs=True,
+                   check=_check_fp16, params=dict(ODD_PARAMS, levels=1))
 
 
 def _ref_pair(dev, spec, n, storage, check):
