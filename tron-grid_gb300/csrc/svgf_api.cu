@@ -137,6 +137,8 @@ size_t col_pixels_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
     return n;
 }
 
+size_t col_guide_half_of(const tg_svgf_params& p, uint32_t w, uint32_t h) { return col_pixels_of(p, w, h); }
+
 size_t col_var_offset_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     return align_up(col_pixels_of(p, w, h) * layout_of(p).rec, 256);
@@ -336,9 +338,9 @@ EncodeTiledFn encode_tiled()
 }
 
 // One tensor map per a-trous level L >= 1 over that level's input records in
-// the residue-major layout of stride 2^L: FP32 {4 floats, record half, column,
-// row, plane}, FP16 {8-byte element (two per record), row, plane}; box = one
-// 36 x 20 halo tile.
+// the residue-major layout of stride 2^L: FP32 {float, row, plane, half-plane},
+// FP16 {8-byte element (two per record), row, plane}; box = one 36 x 20 halo
+// tile, whose rows are contiguous lines.
 // Level 0 has no records: its maps cover the tc and guide planes.
 void build_tensor_maps(tg_svgf* s)
 {
@@ -362,11 +364,12 @@ void build_tensor_maps(tg_svgf* s)
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         } else {
-            const cuuint64_t dim[5] = {4, 2, cuuint64_t(L.pw), cuuint64_t(L.ph), planes};
-            const cuuint64_t str[4] = {16, 32, 32ull * L.pw, 32ull * L.pw * L.ph};
-            const cuuint32_t box[5] = {4, 1, LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1};
-            const cuuint32_t es[5] = {1, 1, 1, 1, 1};
-            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, base, dim, str, box, es,
+            // a row of either half-plane as 4 pw floats: one contiguous 576-byte line per tile row and half
+            const cuuint64_t dim[4] = {4ull * L.pw, cuuint64_t(L.ph), planes, 2};
+            const cuuint64_t str[3] = {16ull * L.pw, 16ull * L.pw * L.ph, 16ull * col_guide_half_of(s->p, s->w, s->h)};
+            const cuuint32_t box[4] = {4 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1, 1};
+            const cuuint32_t es[4] = {1, 1, 1, 1};
+            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dim, str, box, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         }
@@ -582,6 +585,7 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.fallback_frames = s->p.fallback_frames;
         a.col_dst = s->colA;
         a.var_off = col_var_offset_of(s->p, s->w, s->h);
+        a.ghalf = col_guide_half_of(s->p, s->w, s->h);
         const double npx = double(s->w) * s->h;
         const double gb = f16 ? 8 : 16, c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
         const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +

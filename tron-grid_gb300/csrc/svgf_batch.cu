@@ -288,6 +288,7 @@ void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const 
         a.fb_flags = s.fb_flags;
         a.col_dst = s.colA;
         a.var_off = col_var_offset_of(b->p, W, b->h[ids[j]]);
+        a.ghalf = col_guide_half_of(b->p, W, b->h[ids[j]]);
         a.alpha = b->p.alpha;
         a.alpha_m = b->p.moments_alpha;
         a.sigma_l = b->p.sigma_l;

@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
                 lv.col_src = (L & 1) ? e.colB : e.colA;
                 lv.col_dst = (L & 1) ? e.colA : e.colB;
                 lv.var_off = a.var_off;
+                lv.ghalf = a.ghalf;
                 lv.level = L;
                 lv.last = L == hd.levels - 1;
                 lv.lin = res_layout(a.w, a.h, L);
@@ -233,6 +234,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level
     lv.col_src = (L & 1) ? e.colB : e.colA;
     lv.col_dst = (L & 1) ? e.colA : e.colB;
     lv.var_off = a.var_off;
+    lv.ghalf = a.ghalf;
     lv.level = L;
     lv.last = L == hd->levels - 1;
     lv.lin = res_layout(a.w, a.h, L);

@@ -277,20 +277,21 @@ template <> struct Stor<ST_FP32> {
     __device__ static float4 rt4(float4 v) { return v; }
     __device__ static float2 rtm(float2 v) { return v; }
     __device__ static float qin(float v) { return v; }
-    // a-trous scratch record (32 B): float4 (r, g, b, var) then the guide float4 (n, z)
+    // a-trous scratch record (32 B): float4 (r, g, b, var) in the colour half-plane at i, the guide float4
+    // (n, z) in the guide half-plane at gh + i; a tile row of either half is one contiguous run
     typedef float4 rec_t;
     typedef float4 graw_t;
     static constexpr int kRecBytes = 32;
     __device__ static graw_t ld_graw(const guide_t* p, size_t i) { return __ldg(p + i); }
-    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g)
+    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g, size_t gh)
     {
-        c = __ldg(p + 2 * i);
-        g = __ldg(p + 2 * i + 1);
+        c = __ldg(p + i);
+        g = __ldg(p + gh + i);
     }
-    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g)
+    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g, size_t gh)
     {
-        p[2 * i] = c;
-        p[2 * i + 1] = g;
+        p[i] = c;
+        p[gh + i] = g;
     }
     // variance plane beside the records (`off` bytes after the buffer start), 4 B per record
     typedef float var_t;
@@ -358,8 +359,11 @@ template <> struct Stor<ST_FP16> {
         const float3 n = oct16_decode_fast(u.z);
         g = make_float4(n.x, n.y, n.z, __uint_as_float(u.w));
     }
-    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g) { decode_rec(__ldg(p + i), c, g); }
-    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g)
+    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g, size_t)
+    {
+        decode_rec(__ldg(p + i), c, g);
+    }
+    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g, size_t)
     {
         p[i] = make_uint4(pack_h2(c.x, c.y), pack_h2(c.z, sat16(c.w)), g.x, g.y);
     }

@@ -35,6 +35,9 @@ size_t rec_bytes_of(const tg_svgf_params& p);
 size_t col_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 // Byte offset of that variance plane from the start of the buffer.
 size_t col_var_offset_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
+// FP32 FULL records are stored as two half-planes (all colours, then all
+// guides): the index of the guide half-plane in 16-byte units.
+size_t col_guide_half_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 // Bytes of the per-pixel-block fallback flags of a FULL frame.
 size_t fb_flags_bytes_of(uint32_t w, uint32_t h);
 

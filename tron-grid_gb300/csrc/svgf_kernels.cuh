@@ -97,6 +97,7 @@ struct FullArgs {
     const void* col_src;
     void* col_dst;
     size_t var_off;         // byte offset of the variance plane in col_src / col_dst
+    size_t ghalf;           // FP32 records: index of the guide half-plane (16-byte units)
     float2* grad;           // per-pixel depth gradient (written by the temporal kernel)
     int* fb_flags;          // per 32x8 pixel block: 1 if a pixel needs the spatial variance fallback
     int* err;               // device error word (bounded waits that gave up); may be null

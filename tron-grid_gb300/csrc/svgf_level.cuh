@@ -107,6 +107,7 @@ struct LevelArgs {
     const void* col_src;
     void* col_dst;
     size_t var_off;  // byte offset of the variance plane in col_src / col_dst
+    size_t ghalf;    // FP32 records: index of the guide half-plane (16-byte units)
     int level, last;
     ResLayout lin, lout;
 };
@@ -117,6 +118,7 @@ __host__ __device__ inline LevelArgs level_args_of(const FullArgs& a)
     l.col_src = a.col_src;
     l.col_dst = a.col_dst;
     l.var_off = a.var_off;
+    l.ghalf = a.ghalf;
     l.level = a.level;
     l.last = a.last;
     l.lin = a.lin;
@@ -320,7 +322,7 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
             else
                 graw = sm.X1[c];
             const size_t oi = res_idx(lv.lout, cx, y);
-            S::st_rec(static_cast<typename S::rec_t*>(lv.col_dst), oi, o, graw);
+            S::st_rec(static_cast<typename S::rec_t*>(lv.col_dst), oi, o, graw, lv.ghalf);
             S::st_var(lv.col_dst, lv.var_off, oi, o.w);
         }
     }
@@ -377,7 +379,7 @@ __device__ __forceinline__ void level_tile_body(const FullArgs& a, const LevelAr
                 S::decode_rec(u, c, n);
                 oct = u.z;
             } else {
-                S::ld_rec(src, ri, c, n);
+                S::ld_rec(src, ri, c, n, lv.ghalf);
             }
         }
         if constexpr (ST == ST_FP16) sm.XO[k] = oct;
@@ -412,10 +414,10 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_lev
 //
 // The same level with the halo tile staged by the tensor-memory accelerator:
 // one elected thread issues cp.async.bulk.tensor for the tile's box of
-// residue-major records (5-D map {4 floats, record half, column, row, plane}
-// for FP32, so that the box of each record half lands as one dense float4
-// array; for FP16 a 3-D map {8-byte element, row, plane}, so that each tile row
-// of 16-byte records is one contiguous 576-byte line), completion is
+// residue-major records (FP32: 4-D map {float, row, plane, half-plane}, so that
+// the box of each half lands as one dense float4 array and each tile row is one
+// contiguous 576-byte line; FP16: a 3-D map {8-byte element, row, plane}, each
+// tile row of 16-byte records one 576-byte line), completion is
 // tracked by an mbarrier transaction count, and cells outside the plane array
 // arrive zero-filled.  The wait is bounded: a box that has not landed after
 // about a second sets a->err and the CTA returns.
@@ -569,15 +571,16 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
                         : "memory");
             }
         } else if constexpr (ST == ST_FP32) {
+            // x = 4 (i0 - 2) floats: the box starts on a 16-byte boundary
             const uint32_t bytes = 2u * T::N * 16u;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
                 const uint32_t dst = smem_u32(half == 0 ? sm.X0 : sm.X1);
                 asm volatile(
-                    "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
-                    "%6}], [%7];" ::"r"(dst),
-                    "l"(map), "r"(0), "r"(half), "r"(i0 - 2), "r"(j0 - 2), "r"(plane), "r"(ubar)
+                    "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+                    "[%6];" ::"r"(dst),
+                    "l"(map), "r"(4 * (i0 - 2)), "r"(j0 - 2), "r"(plane), "r"(half), "r"(ubar)
                     : "memory");
             }
         } else {

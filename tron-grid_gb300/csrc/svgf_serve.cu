@@ -290,6 +290,7 @@ FullArgs args_for(tg_svgf_server* sv, Sess& s)
     a.fb_flags = s.fb_flags;
     a.col_dst = s.colA;
     a.var_off = col_var_offset_of(sv->d.params, s.w, s.h);
+    a.ghalf = col_guide_half_of(sv->d.params, s.w, s.h);
     const tg_svgf_params& p = sv->d.params;
     a.alpha = p.alpha;
     a.alpha_m = p.moments_alpha;
