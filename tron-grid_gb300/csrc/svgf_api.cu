@@ -376,8 +376,8 @@ void build_tensor_maps(tg_svgf* s)
         if (r != CUDA_SUCCESS) return;
     }
     s->tma = true;
-    // Level 0's planes: FP32 {4 floats, column, row}, FP16 {8-byte texel, column, row} (its row pitch must be a
-    // multiple of 16 bytes, so an odd width stages level 0 with plain loads).
+    // Level 0's planes: FP32 {float, row}, FP16 {8-byte texel, row} (its row pitch must be a multiple of 16 bytes,
+    // so an odd width stages level 0 with plain loads); each tile row is one contiguous line.
     s->tma0 = false;
     void* planes[3] = {s->tc, s->guide[0], s->guide[1]};
     CUtensorMap* maps[3] = {&s->tm_tc, &s->tm_guide[0], &s->tm_guide[1]};
@@ -392,11 +392,11 @@ void build_tensor_maps(tg_svgf* s)
             r = enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, planes[k], dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         } else {
-            const cuuint64_t dim[3] = {4, s->w, s->h};
-            const cuuint64_t str[2] = {16, 16ull * s->w};
-            const cuuint32_t box[3] = {4, LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH};
-            const cuuint32_t es[3] = {1, 1, 1};
-            r = enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, planes[k], dim, str, box, es,
+            const cuuint64_t dim[2] = {4ull * s->w, s->h};
+            const cuuint64_t str[1] = {16ull * s->w};
+            const cuuint32_t box[2] = {4 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH};
+            const cuuint32_t es[2] = {1, 1};
+            r = enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, planes[k], dim, str, box, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         }

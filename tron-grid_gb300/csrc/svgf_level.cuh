@@ -450,8 +450,8 @@ struct NoRaw {};
 
 // PL (level 0): the box comes from two row-major images
 // instead of the records, tc through `tm` and guide_cur through `tm2` (FP32:
-// 3-D maps {4 floats, column, row} landing as X0 and X1; FP16: 2-D maps of
-// 8-byte texels landing in PlaneRaw16); each staged cell's variance comes from
+// 2-D maps {float, row} landing as X0 and X1; FP16: 2-D maps of 8-byte texels
+// landing in PlaneRaw16); each staged cell's variance comes from
 // the variance plane, loaded before the wait.
 // The TMA kernel after its copy is issued: prefetch, bounded wait, fix-up,
 // compute.  IN: the tile is interior (tile_interior), so no cell needs a test.
@@ -562,12 +562,13 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
                         "l"(h == 0 ? map : map2), "r"(i0 - 2), "r"(j0 - 2), "r"(ubar)
                         : "memory");
             } else {
+                // x = 4 (i0 - 2) floats: the box starts on a 16-byte boundary
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
                     asm volatile(
-                        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
-                        "%4}], [%5];" ::"r"(smem_u32(h == 0 ? sm.X0 : sm.X1)),
-                        "l"(h == 0 ? map : map2), "r"(0), "r"(i0 - 2), "r"(j0 - 2), "r"(ubar)
+                        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                        "[%4];" ::"r"(smem_u32(h == 0 ? sm.X0 : sm.X1)),
+                        "l"(h == 0 ? map : map2), "r"(4 * (i0 - 2)), "r"(j0 - 2), "r"(ubar)
                         : "memory");
             }
         } else if constexpr (ST == ST_FP32) {
