@@ -127,23 +127,17 @@ template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArg
     prefetch_l2(static_cast<const G*>(a.guide_prev) + i);
     prefetch_l2(static_cast<const M*>(a.mom_prev) + i);
 
+    // Every load of this pixel is issued before its first store (the motion first: the reprojection gathers
+    // depend on it), and the gathers before the guide and gradient work, which runs while they are in flight.
+    const float2 mv = ld_motion(a.motion, x, y);
+    const float4 c4 = ld_rgba(a.radiance, x, y);
     uint32_t enc = 0;
     float3 n = ld_normal(a.normal, x, y, ST == ST_FP16, enc);
-    if (ST == ST_FP16) n = oct16_decode_raw(enc);  // FP16 storage keeps the octahedral code
     const float z = ld_depth(a.depth, x, y);
-    const G gv = S::mk_guide(n, enc, z);
-    static_cast<G*>(a.guide_cur)[i] = gv;
-
     const bool hl = x > 0, hr = x < a.w - 1, hu = y > 0, hd = y < a.h - 1;
-    const float gx = grad1(z, hl ? ld_depth(a.depth, x - 1, y) : 0.0f, hr ? ld_depth(a.depth, x + 1, y) : 0.0f, hl, hr);
-    const float gy = grad1(z, hu ? ld_depth(a.depth, x, y - 1) : 0.0f, hd ? ld_depth(a.depth, x, y + 1) : 0.0f, hu, hd);
+    const float zl = hl ? ld_depth(a.depth, x - 1, y) : 0.0f, zr = hr ? ld_depth(a.depth, x + 1, y) : 0.0f;
+    const float zu = hu ? ld_depth(a.depth, x, y - 1) : 0.0f, zd = hd ? ld_depth(a.depth, x, y + 1) : 0.0f;
 
-    a.grad[i] = make_float2(gx, gy);
-    const float4 c4 = ld_rgba(a.radiance, x, y);
-    const float cr = S::qin(c4.x), cg = S::qin(c4.y), cb = S::qin(c4.z);
-    const float gsum = __fadd_rn(fabsf(gx), fabsf(gy));
-    const float ztol = __fadd_rn(__fadd_rn(__fmul_rn(kDepthRel, z), __fmul_rn(kDepthGrad, gsum)), kDepthAbs);
-    const float2 mv = ld_motion(a.motion, x, y);
     const float px = __fadd_rn(float(x), mv.x);
     const float py = __fadd_rn(float(y), mv.y);
     const float fx0 = floorf(px), fy0 = floorf(py);
@@ -181,6 +175,16 @@ template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArg
             tm[k] = make_float2(0.f, 0.f);
         }
     }
+
+    if (ST == ST_FP16) n = oct16_decode_raw(enc);  // FP16 storage keeps the octahedral code
+    const G gv = S::mk_guide(n, enc, z);
+    static_cast<G*>(a.guide_cur)[i] = gv;
+    const float gx = grad1(z, zl, zr, hl, hr);
+    const float gy = grad1(z, zu, zd, hu, hd);
+    a.grad[i] = make_float2(gx, gy);
+    const float cr = S::qin(c4.x), cg = S::qin(c4.y), cb = S::qin(c4.z);
+    const float gsum = __fadd_rn(fabsf(gx), fabsf(gy));
+    const float ztol = __fadd_rn(__fadd_rn(__fmul_rn(kDepthRel, z), __fmul_rn(kDepthGrad, gsum)), kDepthAbs);
     float sw = 0.0f, hr_ = 0.0f, hg = 0.0f, hb = 0.0f, hmu = 0.0f;
     float tw[4];
     int lmax = 0;
