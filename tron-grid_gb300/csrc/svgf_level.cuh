@@ -295,7 +295,14 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
     }
 
     // Outputs: the next level's record (colour, variance, the centre's guide),
-    // the colour history at level 0, the caller's image at the last level.
+    // the colour history at level 0, the caller's image at the last level.  At
+    // level 0 the history lengths of all outputs are loaded before any store.
+    float len[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int y = rb + s * (j0 + cj0 + k);
+        len[k] = (lv.level == 0 && pre.valid[k]) ? S::ld4_w(static_cast<const C4*>(a.tc), y * a.w + cx) : 0.f;
+    }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (!pre.valid[k]) continue;
@@ -309,10 +316,7 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
         } else {
             o = sm.X0[c];
         }
-        if (lv.level == 0) {
-            const float len = S::ld4_w(static_cast<const C4*>(a.tc), i);
-            S::st4(static_cast<C4*>(a.hist_cur), i, make_float4(o.x, o.y, o.z, len));
-        }
+        if (lv.level == 0) S::st4(static_cast<C4*>(a.hist_cur), i, make_float4(o.x, o.y, o.z, len[k]));
         if (lv.last) {
             st_rgba(a.out, cx, y, make_float4(S::qin(o.x), S::qin(o.y), S::qin(o.z), 1.0f));
         } else {
