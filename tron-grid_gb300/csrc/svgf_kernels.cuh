@@ -263,18 +263,18 @@ struct VarTile {
     float2 m[kVarTH * kVarTW];  // luminance mean, variance
 };
 
+// `t` (the pixel's temporal colour and length) and `gr` (its depth gradient)
+// are loaded by the caller before it stages the tile.
 template <int ST>
-__device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y, int cell, const VarTile& vt)
+__device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y, int cell, const VarTile& vt, float4 t,
+                                                 float2 gr)
 {
     typedef Stor<ST> S;
-    typedef typename S::c4_t C4;
     const size_t i = size_t(y) * a.w + x;
-    const float4 t = S::ld4(static_cast<const C4*>(a.tc), i);
     const int len = int(t.w);
     if (len >= a.fallback_frames) return;
     const float2 mom = vt.m[cell];
     const float4 g = vt.g[cell];
-    const float2 gr = a.grad[i];
     // w = max(0, n.n')^sigma_n exp(-|dz| / (sigma_z |grad z . off| + eps_z)), as one ex2;
     // offsets (dx, dy) and (-dx, -dy) share the depth scale kz
     const float A_ = a.sigma_z * gr.x * (1.0f / kLog2eF), B_ = a.sigma_z * gr.y * (1.0f / kLog2eF);
@@ -334,6 +334,11 @@ template <int ST> __device__ __forceinline__ void full_variance_tile(const FullA
     const int x0 = x - int(threadIdx.x) - kVarHalo, y0 = y - int(threadIdx.y) - kVarHalo;
     const typename S::guide_t* gc = static_cast<const typename S::guide_t*>(a.guide_cur);
     const typename S::mom_t* mc = static_cast<const typename S::mom_t*>(a.mom_cur);
+    // this thread's own pixel inputs, loaded before the staging so that their latency overlaps it
+    const bool own = x < a.w && y < a.h;
+    const size_t i = own ? size_t(y) * a.w + x : 0;
+    const float4 t = own ? S::ld4(static_cast<const typename S::c4_t*>(a.tc), i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 gr = own ? a.grad[i] : make_float2(0.f, 0.f);
     for (int k = threadIdx.y * kBlockX + threadIdx.x; k < kVarTH * kVarTW; k += kBlockX * kBlockY) {
         const int qy = y0 + k / kVarTW, qx = x0 + k % kVarTW;
         float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -347,8 +352,7 @@ template <int ST> __device__ __forceinline__ void full_variance_tile(const FullA
         vt.m[k] = m;
     }
     __syncthreads();
-    if (x < a.w && y < a.h)
-        full_variance_px<ST>(a, x, y, (int(threadIdx.y) + kVarHalo) * kVarTW + int(threadIdx.x) + kVarHalo, vt);
+    if (own) full_variance_px<ST>(a, x, y, (int(threadIdx.y) + kVarHalo) * kVarTW + int(threadIdx.x) + kVarHalo, vt, t, gr);
     __syncthreads();  // the tile's storage is reused by the caller's next block
 }
 
