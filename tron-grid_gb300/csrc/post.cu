@@ -372,7 +372,7 @@ int tg_post_process(tg_post* s, const tg_image* hdr, const tg_image* out, void* 
     if (!s) return fail(TG_ERR_INVALID, "null handle");
     static const int kHdr[] = {TG_FMT_RGBA16F, TG_FMT_RGBA32F};
     static const int kOut[] = {TG_FMT_BGRA8, TG_FMT_RGBA8, TG_FMT_RGBA32F};
-    long long hp, op;
+    long long hp = 0, op = 0;
     int st;
     if ((st = check_img("hdr", hdr, s->w, kHdr, 2, hp))) return st;
     if ((st = check_img("out", out, s->w, kOut, 3, op))) return st;
