@@ -452,11 +452,6 @@ template <int R> struct __align__(128) PlaneRaw16 {
 };
 struct NoRaw {};
 
-// PL (level 0): the box comes from two row-major images
-// instead of the records, tc through `tm` and guide_cur through `tm2` (FP32:
-// 2-D maps {float, row} landing as X0 and X1; FP16: 2-D maps of 8-byte texels
-// landing in PlaneRaw16); each staged cell's variance comes from
-// the variance plane, loaded before the wait.
 // The TMA kernel after its copy is issued: prefetch, bounded wait, fix-up,
 // compute.  IN: the tile is interior (tile_interior), so no cell needs a test.
 template <int ST, int R, bool VAR, bool PL, bool IN, class Raw16>
@@ -526,6 +521,12 @@ __device__ __forceinline__ void tma_tile_body(const FullArgs& a, const LevelArgs
     level_compute<ST, R, VAR, IN>(a, lv, g, ra, rb, i0, j0, pre, sm);
 }
 
+// One level with its tile staged by TMA.  VAR = false at the last level (colour
+// only).  PL (level 0): the box comes from two row-major images instead of the
+// records, tc through `tm` and guide_cur through `tm2` (FP32: 2-D maps
+// {float, row} landing as X0 and X1; FP16: 2-D maps of 8-byte texels landing
+// in PlaneRaw16), and each staged cell's variance comes from the variance
+// plane, loaded before the wait.  Other levels read `tm` only.
 template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm,
