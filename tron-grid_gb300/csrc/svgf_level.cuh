@@ -214,6 +214,12 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
     const int s = g.s;
     const int ci = threadIdx.x, cj0 = threadIdx.y * R;
     const int cx = ra + s * (i0 + ci);
+    // A warp (one strip row of 32 columns) whose outputs all lie outside the
+    // sub-lattice has nothing to compute or write.
+    bool any_valid = false;
+#pragma unroll
+    for (int k = 0; k < R; ++k) any_valid |= pre.valid[k];
+    if (!__any_sync(0xffffffffu, any_valid)) return;
     float lp[R], kl[R], zp[R], nx[R], ny[R], nz[R], kz[R][13];
     float ar[R], ag[R], ab[R], aw[R], av[R];
     const float zs = a.sigma_z * float(s) * (1.0f / kLog2e);
@@ -257,14 +263,9 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
         }
     }
 
-    // Taps: rows r = 0 .. R+3 of this thread's strip, 5 columns each.  A warp
-    // (one strip row of 32 columns) whose outputs all lie outside the
-    // sub-lattice skips them.
-    bool any_valid = false;
-#pragma unroll
-    for (int k = 0; k < R; ++k) any_valid |= pre.valid[k];
+    // Taps: rows r = 0 .. R+3 of this thread's strip, 5 columns each.
     const float sn = a.sigma_n;
-    if (__any_sync(0xffffffffu, any_valid)) {
+    {
 #pragma unroll
         for (int r = 0; r < R + 4; ++r) {
 #pragma unroll
