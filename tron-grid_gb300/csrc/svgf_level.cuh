@@ -623,6 +623,18 @@ template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref
     const int s = g.s;
     const C4* src = static_cast<const C4*>(a.src);
     const int tid = threadIdx.y * kLvTX + threadIdx.x;
+    const int ci = threadIdx.x, cj0 = threadIdx.y * R;
+    // each centre's alpha (the sigma of its luminance weight), loaded before the staging so that its latency
+    // overlaps it
+    float ca[R];
+    bool valid[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int x = ra + s * (i0 + ci);
+        const int y = rb + s * (j0 + cj0 + k);
+        valid[k] = x < a.w && y < a.h;
+        ca[k] = valid[k] ? S::ld4_w(src, res_idx(a.lin, x, y)) : 0.f;
+    }
     for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
         const int si = k % T::SW, sj = k / T::SW;
         const int x = min(max(ra + s * (i0 + si - 2), 0), a.w - 1);
@@ -632,16 +644,10 @@ template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref
     }
     __syncthreads();
 
-    const int ci = threadIdx.x, cj0 = threadIdx.y * R;
-    float lp[R], nk[R], ca[R], ar[R], ag[R], ab[R], aw[R];
-    bool valid[R];
+    float lp[R], nk[R], ar[R], ag[R], ab[R], aw[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        const int x = ra + s * (i0 + ci);
-        const int y = rb + s * (j0 + cj0 + k);
-        valid[k] = x < a.w && y < a.h;
         lp[k] = sA[(cj0 + k + 2) * T::SW + ci + 2].w;
-        ca[k] = valid[k] ? S::ld4_w(src, res_idx(a.lin, x, y)) : 0.f;
         const float sigma = fmaxf(__fmul_rn(a.phi, ca[k]), a.var_eps);
         nk[k] = -kLog2e / sigma;
         ar[k] = ag[k] = ab[k] = aw[k] = 0.f;
