@@ -170,18 +170,27 @@ def test_ref_exact_odd_sizes(cuda_dev, wh):
     _ref_pair(cuda_dev, scene.SceneSpec(wh[0], wh[1], seed=8), 4, tg.STORAGE_FP32, chk)
 
 
-def test_host_api_matches_device_api(cuda_dev):
+@pytest.mark.parametrize("storage", [tg.STORAGE_FP32, tg.STORAGE_FP16])
+def test_host_api_matches_device_api(cuda_dev, storage):
+    """tg_svgf_denoise_host (pinned host buffers, four frames through its ring of three staging sets) gives the
+    device API's bits; FP16 storage with rgba16f radiance and octahedral normals."""
     spec = scene.config1(200, 120, seed=9)
     frames = _frames(spec, 4)
-    a = tg.Denoiser(200, 120)
-    b = tg.Denoiser(200, 120)
+    f16 = storage == tg.STORAGE_FP16
+    if f16:
+        for fr in frames:
+            fr["radiance"] = fr["radiance"].half()
+            fr["normal"] = torch.from_numpy(oracle.oct16_encode(fr["normal"].numpy()))
+    dt = torch.float16 if f16 else torch.float32
+    a = tg.Denoiser(200, 120, storage=storage)
+    b = tg.Denoiser(200, 120, storage=storage)
     outs_h = []
     for fr in frames:
         ins = [fr[k].pin_memory() for k in KEYS]
-        outs_h.append(b.denoise_host(*ins))
+        outs_h.append(b.denoise_host(*ins, out=torch.empty((120, 200, 4), dtype=dt, pin_memory=True)))
     b.synchronize()
     for fr, oh in zip(frames, outs_h):
-        od = a.denoise(*(fr[k].to(cuda_dev) for k in KEYS))
+        od = a.denoise(*(fr[k].to(cuda_dev) for k in KEYS), out=torch.empty((120, 200, 4), dtype=dt, device=cuda_dev))
         assert torch.equal(od.cpu(), oh)
     a.close()
     b.close()
