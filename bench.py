@@ -312,7 +312,9 @@ def run_tg(args, rank, world, local):
             tr = traffic["dram_bytes_per_px"] * px
         res["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                            "frac": achieved / peak, "traffic": tr,
-                           "algo_bytes_per_launch": d["algo_bytes"] / d["launches"], "peak_source": peak_src}
+                           "algo_bytes_per_launch": d["algo_bytes"] / d["launches"], "peak_source": peak_src,
+                           # the compute side of the same kernel: issue slots busy in the ncu capture of profiles/
+                           "issue_active_pct": traffic.get("issue_active_pct") if traffic else None}
         res["kernels"] = kern
     res["clocks"] = clk
     den.close()
