@@ -155,6 +155,40 @@ def test_full_constant_image_is_fixed_point():
         assert np.all(np.abs(var) < 1e-20)
 
 
+@pytest.mark.parametrize("levels", [1, 2, 3, 4, 5])
+def test_full_constant_image_is_fixed_point_at_every_level_count(levels):
+    """A constant image stays itself through any number of a-trous levels, with non-default edge-stop widths."""
+    h, w = 9, 13
+    p = oracle.full_params(levels=levels, sigma_l=2.5, sigma_n=64.0, sigma_z=0.5)
+    st = oracle.FullState(h, w)
+    for t in range(4):
+        rad, dep, nrm, mot = _static_inputs(h, w, (0.9, 0.3, 0.6))
+        out, var = oracle.full_frame(p, st, rad, dep, nrm, mot)
+        np.testing.assert_allclose(out[..., :3], rad[..., :3], rtol=1e-13)
+        assert np.all(out[..., 3] == 1.0) and np.all(np.abs(var) < 1e-20)
+
+
+@pytest.mark.parametrize("fallback", [1, 3, 4])
+def test_full_fallback_window(fallback):
+    """Below `fallback_frames` of history the level-0 variance is the 7x7 spatial estimate, from then on the pixel's
+    temporal variance exactly (static camera: the history grows by one each frame).  With no a-trous level the
+    oracle returns that level-0 variance itself."""
+    h, w = 12, 15
+    p = oracle.full_params(fallback_frames=fallback, levels=0)
+    st = oracle.FullState(h, w)
+    rng = np.random.default_rng(fallback)
+    for t in range(6):
+        rad, dep, nrm, mot = _static_inputs(h, w, (0.5, 0.5, 0.5))
+        rad[..., :3] *= rng.exponential(1.0, (h, w, 1))
+        _, var = oracle.full_frame(p, st, rad, dep, nrm, mot)
+        assert np.all(st.hist[..., 3] == t + 1)
+        if t + 1 >= fallback:
+            np.testing.assert_array_equal(var, st.mom[..., 1])
+        else:
+            assert not np.allclose(var, st.mom[..., 1])
+            assert np.all(var >= 0.0) and np.all(np.isfinite(var))
+
+
 def test_full_history_length_caps_and_disocclusion_resets():
     h, w = 6, 7
     p = oracle.full_params(max_history=5)
