@@ -86,16 +86,47 @@ def test_missing_library_fails_loudly(tmp_path):
 
 
 def test_cpp_wrapper_compiles(tmp_path):
+    """The C++ RAII wrappers compile, and - linked against the built library on a host without a GPU - every one
+    turns its handle's failure into a tg::Error carrying the C status (nothing throws across the C ABI)."""
     import shutil
     import subprocess
 
     if not shutil.which("g++"):
         pytest.skip("no g++")
     src = tmp_path / "use.cpp"
-    src.write_text('#include "tg_svgf.hpp"\nint main() { try { tg::SvgfDenoiser d(16, 16); } catch (const tg::Error&) {} }\n')
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
-                       capture_output=True, text=True)
+    src.write_text('#include "tg_svgf.hpp"\n'
+                   '#include <cstdio>\n'
+                   'int main() {\n'
+                   '  int caught = 0;\n'
+                   '  try { tg::SvgfDenoiser d(16, 16); } catch (const tg::Error& e) { caught += e.status() != 0; }\n'
+                   '  try { tg::PostProcessor pp(16, 8); tg_image hdr{}, out{}; pp.process(hdr, out); }\n'
+                   '  catch (const tg::Error& e) { caught += e.status() != 0; }\n'
+                   '  uint32_t w = 8, h = 8;\n'
+                   '  tg_eye_desc ed{};\n'
+                   '  ed.n_eyes = 1; ed.widths = &w; ed.heights = &h; ed.ring = 3; ed.device = -1;\n'
+                   '  try { tg::EyeReadback er(ed); tg_vision_data v[1]; er.acquire(0, v); }\n'
+                   '  catch (const tg::Error& e) { caught += e.status() != 0; }\n'
+                   '  tg_fog_filter_params fp{};\n'
+                   '  tg_volume a{}, b{}, c{};\n'
+                   '  try { tg::fog_filter(fp, a, b, c); } catch (const tg::Error& e) { caught += e.status() == TG_ERR_INVALID; }\n'
+                   '  std::printf("%d\\n", caught);\n'
+                   '  return 0;\n'
+                   '}\n')
+    inc = os.path.join(ROOT, "include")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", inc, str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+    import torch
+
+    lib_dir = os.path.join(ROOT, "tron-grid_gb300", "lib")
+    if torch.cuda.is_available() or not os.path.exists(os.path.join(lib_dir, "libtg_svgf.so")):
+        return  # the failure path below needs a host without a GPU and the built library
+    exe = tmp_path / "use"
+    r = subprocess.run(["g++", "-std=c++17", "-I", inc, str(src), "-o", str(exe), "-L", lib_dir, "-ltg_svgf",
+                        f"-Wl,-rpath,{lib_dir}", "-Wl,-rpath,/usr/local/cuda/lib64"], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip(f"could not link against the library: {r.stderr[-300:]}")
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "4", (r.stdout, r.stderr)
 
 
 def test_server_and_batch_reject_bad_descriptors_on_the_host():
