@@ -52,28 +52,48 @@ def full_params(alpha=0.2, moments_alpha=0.2, sigma_l=4.0, sigma_n=128.0, sigma_
     return FullParams(alpha, moments_alpha, sigma_l, sigma_n, sigma_z, levels, max_history, fallback_frames, 0)
 
 
-def _lib():
-    global _orc
+_orc_timing = None
+
+
+def _lib(timing: bool = False):
+    """The checker build, or with ``timing`` the timed CPU baseline's build (oracle/build.py TIMING_CXXFLAGS)."""
+    global _orc, _orc_timing
+    if timing:
+        if _orc_timing is None:
+            path = _build.ORC_TIMING_LIB
+            if not os.path.exists(path):
+                path = _build.build_oracle_timing()
+            _orc_timing = _declare(C.CDLL(path))
+        return _orc_timing
     if _orc is None:
         path = _build.ORC_LIB
         if not os.path.exists(path):
             path = _build.build_oracle()
-        _orc = C.CDLL(path)
-        P = C.c_void_p
-        _orc.orc_ref_frame_f32.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_float, C.c_float, C.c_float,
-                                           C.c_int, C.c_int]
-        _orc.orc_ref_frame_f64.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_double, C.c_double,
-                                           C.c_double, C.c_int, C.c_int]
-        for nm in ("orc_full_frame_f32", "orc_full_frame_f64"):
-            getattr(_orc, nm).argtypes = [C.POINTER(FullParams), C.c_int, C.c_int] + [P] * 12 + [C.c_int, C.c_int]
-        _orc.orc_oct16_encode.argtypes = [C.c_int, P, P]
-        _orc.orc_oct16_decode.argtypes = [C.c_int, P, P]
-        _orc.orc_num_threads.restype = C.c_int
-        _orc.orc_fog_filter.argtypes = [C.c_char_p, P, P, P, C.c_int, C.c_int, C.c_int]
-        _orc.orc_post_frame.argtypes = [C.c_int, C.c_int, P, C.c_float, C.c_float, C.c_int, P, P, C.c_int, C.c_int,
-                                        C.c_int, C.c_int]
-        _orc.orc_post_frame.restype = C.c_int
+        _orc = _declare(C.CDLL(path))
     return _orc
+
+
+def timing_flags() -> str:
+    return " ".join(_build.TIMING_CXXFLAGS)
+
+
+def _declare(lib):
+    """Argument types of the oracle's C entry points (the same in both builds)."""
+    P = C.c_void_p
+    lib.orc_ref_frame_f32.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_float, C.c_float, C.c_float,
+                                      C.c_int, C.c_int]
+    lib.orc_ref_frame_f64.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_double, C.c_double,
+                                      C.c_double, C.c_int, C.c_int]
+    for nm in ("orc_full_frame_f32", "orc_full_frame_f64"):
+        getattr(lib, nm).argtypes = [C.POINTER(FullParams), C.c_int, C.c_int] + [P] * 12 + [C.c_int, C.c_int]
+    lib.orc_oct16_encode.argtypes = [C.c_int, P, P]
+    lib.orc_oct16_decode.argtypes = [C.c_int, P, P]
+    lib.orc_num_threads.restype = C.c_int
+    lib.orc_fog_filter.argtypes = [C.c_char_p, P, P, P, C.c_int, C.c_int, C.c_int]
+    lib.orc_post_frame.argtypes = [C.c_int, C.c_int, P, C.c_float, C.c_float, C.c_int, P, P, C.c_int, C.c_int,
+                                   C.c_int, C.c_int]
+    lib.orc_post_frame.restype = C.c_int
+    return lib
 
 
 def reference_available() -> bool:
@@ -110,14 +130,15 @@ def _p(a):
 
 
 def ref_frame(raw, mom_prev, levels=3, phi=2.0, alpha_m=0.2, var_eps=1e-4, fp16_store=True, dtype=np.float32,
-              threads=0):
+              threads=0, timing=False):
     """One reference frame.  raw (h,w,4), mom_prev (h,w,2) -> (out (h,w,4), mom_curr (h,w,2))."""
     raw = _c(raw, dtype)
     mom_prev = _c(mom_prev, dtype)
     h, w = raw.shape[:2]
     out = np.zeros((h, w, 4), dtype)
     mom = np.zeros((h, w, 2), dtype)
-    f = _lib().orc_ref_frame_f32 if dtype == np.float32 else _lib().orc_ref_frame_f64
+    lib = _lib(timing)
+    f = lib.orc_ref_frame_f32 if dtype == np.float32 else lib.orc_ref_frame_f64
     rc = f(w, h, _p(raw), _p(mom_prev), _p(mom), _p(out), levels, phi, alpha_m, var_eps, int(bool(fp16_store)),
            threads)
     if rc:
@@ -150,8 +171,26 @@ class FullState:
         self.mom = np.zeros((h, w, 2), dtype)
 
 
-def full_frame(params: FullParams, state: FullState, radiance, depth, normal, motion, fp16_store=False, threads=0):
-    """One FULL frame; updates ``state`` in place and returns (out (h,w,4), var (h,w))."""
+# Stores of the FULL algorithm that FP16 storage rounds (the Q_* mask of oracle/svgf_oracle.cpp): each can be
+# emulated on its own to measure its share of the error against float64.
+Q_INPUT, Q_NORMAL, Q_TC, Q_HIST, Q_MOM, Q_RECORD, Q_OUTPUT = 1, 2, 4, 8, 16, 32, 64
+Q_ALL = 127
+
+
+def fp16_storage_mask(fp16_output: bool) -> int:
+    """The stores the CUDA path's FP16 storage form rounds: radiance, octahedral normals, the temporally integrated
+    colour, history and moments in binary16; the a-trous scratch records stay float32; the output is rounded only
+    when the caller's output image is RGBA16F."""
+    return (Q_ALL & ~(Q_RECORD | Q_OUTPUT)) | (Q_OUTPUT if fp16_output else 0)
+
+
+def full_frame(params: FullParams, state: FullState, radiance, depth, normal, motion, fp16_store=False, threads=0,
+               timing=False):
+    """One FULL frame; updates ``state`` in place and returns (out (h,w,4), var (h,w)).
+
+    ``fp16_store``: False / 0 = no emulation, True = every store of the FP16 storage form (Q_ALL), or a mask of
+    Q_* bits naming the stores to round.  ``timing``: run the timed CPU baseline's build instead of the checker's."""
+    mask = (Q_ALL if fp16_store else 0) if isinstance(fp16_store, (bool, np.bool_)) else int(fp16_store)
     dt = state.guide.dtype
     radiance = _c(radiance, dt)
     depth = _c(depth, dt)
@@ -163,9 +202,10 @@ def full_frame(params: FullParams, state: FullState, radiance, depth, normal, mo
     m = np.zeros_like(state.mom)
     out = np.zeros((h, w, 4), dt)
     var = np.zeros((h, w), dt)
-    f = _lib().orc_full_frame_f32 if dt == np.float32 else _lib().orc_full_frame_f64
+    lib = _lib(timing)
+    f = lib.orc_full_frame_f32 if dt == np.float32 else lib.orc_full_frame_f64
     rc = f(C.byref(params), w, h, _p(radiance), _p(depth), _p(normal), _p(motion), _p(state.guide), _p(state.hist),
-           _p(state.mom), _p(g), _p(hs), _p(m), _p(out), _p(var), int(bool(fp16_store)), threads)
+           _p(state.mom), _p(g), _p(hs), _p(m), _p(out), _p(var), mask, threads)
     if rc:
         raise ValueError("oracle full_frame rejected its arguments")
     state.guide, state.hist, state.mom = g, hs, m

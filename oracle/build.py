@@ -44,9 +44,26 @@ FOG_REF_GEN = os.path.join(REF_DIR, "volumetric_filter_gen.cpp")
 POST_REF_LIB = os.path.join(REF_DIR, "libpost_ref.so")
 BLOOM_REF_GEN = os.path.join(REF_DIR, "bloom_downsample_gen.cpp")
 PP_REF_GEN = os.path.join(REF_DIR, "postprocess_gen.cpp")
-DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
+def default_reference_root() -> str:
+    """The reference checkout to translate: $TG_REFERENCE_ROOT, else a directory named `reference` beside this
+    repository's own directory.  Where neither exists the translations are skipped."""
+    env = os.environ.get("TG_REFERENCE_ROOT")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
 
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"]
+# The timed CPU baseline is built for speed, not for bit-agreement with the GPU's discrete decisions: fused
+# multiply-adds allowed, no errno from the math library, unrolled loops.  Host code must build the same way on
+# x86-64 and aarch64 hosts, so no -march=native: both targets' baselines already have fused multiply-add
+# (aarch64) or SSE2 vectors (x86-64), and the restatement is a per-pixel loop over rows that OpenMP spreads over
+# every host core.
+TIMING_CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=fast", "-fno-math-errno",
+                   "-funroll-loops"]
+ORC_TIMING_LIB = os.path.join(BUILD_DIR, "liborc_timing.so")
 
 
 def _newer(target: str, *sources: str) -> bool:
@@ -56,14 +73,31 @@ def _newer(target: str, *sources: str) -> bool:
     return all(os.path.getmtime(s) <= t for s in sources if os.path.exists(s))
 
 
+def _oracle_sources():
+    return [os.path.join(HERE, "svgf_oracle.cpp"), os.path.join(HERE, "fog_oracle.cpp"),
+            os.path.join(HERE, "post_oracle.cpp")]
+
+
 def build_oracle(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, "svgf_oracle.cpp"), os.path.join(HERE, "fog_oracle.cpp"), os.path.join(HERE, "post_oracle.cpp")]
+    """The checker build (liborc.so): no contraction, so that its discrete decisions match the GPU's."""
+    srcs = _oracle_sources()
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if force or not _newer(ORC_LIB, *srcs):
+    if force or not _newer(ORC_LIB, *srcs, __file__):
         tmp = ORC_LIB + ".tmp"
         subprocess.check_call(["g++", *CXXFLAGS, *srcs, "-o", tmp])
         os.replace(tmp, ORC_LIB)
     return ORC_LIB
+
+
+def build_oracle_timing(force: bool = False) -> str:
+    """The timed CPU baseline's build (liborc_timing.so) of the same sources, with TIMING_CXXFLAGS."""
+    srcs = _oracle_sources()
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not _newer(ORC_TIMING_LIB, *srcs, __file__):
+        tmp = ORC_TIMING_LIB + ".tmp"
+        subprocess.check_call(["g++", *TIMING_CXXFLAGS, *srcs, "-o", tmp])
+        os.replace(tmp, ORC_TIMING_LIB)
+    return ORC_TIMING_LIB
 
 
 _FLOAT_LITERAL = re.compile(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
@@ -92,8 +126,9 @@ def _write_if_changed(path: str, text: str) -> None:
             f.write(text)
 
 
-def translate_fog_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+def translate_fog_reference(reference_root: str | None = None) -> str | None:
     """Write oracle/_ref/volumetric_filter_gen.cpp from the reference shader, if present."""
+    reference_root = reference_root or default_reference_root()
     shader = os.path.join(reference_root, "src", "volumetric_filter.slang")
     if not os.path.isfile(shader):
         return None
@@ -104,8 +139,9 @@ def translate_fog_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str
     return FOG_REF_GEN
 
 
-def translate_post_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> bool:
+def translate_post_reference(reference_root: str | None = None) -> bool:
     """Write oracle/_ref/{bloom_downsample,postprocess}_gen.cpp from the reference shaders, if present."""
+    reference_root = reference_root or default_reference_root()
     for name, gen, entries in (("bloom_downsample.slang", BLOOM_REF_GEN, 3), ("postprocess.slang", PP_REF_GEN, 1)):
         shader = os.path.join(reference_root, "src", name)
         if not os.path.isfile(shader):
@@ -117,7 +153,7 @@ def translate_post_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> bo
     return True
 
 
-def build_post_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+def build_post_reference(force: bool = False, reference_root: str | None = None) -> str | None:
     """Compile the translated bloom / post-process shaders; None when no translation exists."""
     translate_post_reference(reference_root)
     if not (os.path.isfile(BLOOM_REF_GEN) and os.path.isfile(PP_REF_GEN)):
@@ -131,7 +167,7 @@ def build_post_reference(force: bool = False, reference_root: str = DEFAULT_REFE
     return POST_REF_LIB
 
 
-def build_fog_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+def build_fog_reference(force: bool = False, reference_root: str | None = None) -> str | None:
     """Compile the translated froxel-filter shader; None when no translation exists."""
     translate_fog_reference(reference_root)
     if not os.path.isfile(FOG_REF_GEN):
@@ -145,8 +181,9 @@ def build_fog_reference(force: bool = False, reference_root: str = DEFAULT_REFER
     return FOG_REF_LIB
 
 
-def translate_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+def translate_reference(reference_root: str | None = None) -> str | None:
     """Write oracle/_ref/svgf_denoise_gen.cpp from the reference shader, if present."""
+    reference_root = reference_root or default_reference_root()
     shader = os.path.join(reference_root, "src", "svgf_denoise.slang")
     if not os.path.isfile(shader):
         return None
@@ -173,7 +210,7 @@ def translate_reference(reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | N
     return REF_GEN
 
 
-def build_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE_ROOT) -> str | None:
+def build_reference(force: bool = False, reference_root: str | None = None) -> str | None:
     """Compile the translated reference shader; None when no translation exists."""
     translate_reference(reference_root)
     if not os.path.isfile(REF_GEN):
@@ -189,10 +226,11 @@ def build_reference(force: bool = False, reference_root: str = DEFAULT_REFERENCE
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-root", default=DEFAULT_REFERENCE_ROOT)
+    ap.add_argument("--reference-root", default=None)
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args(argv)
     print(build_oracle(a.force))
+    print(build_oracle_timing(a.force))
     r = build_reference(a.force, a.reference_root)
     print(r if r else "reference shader translation absent: oracle/_ref not built")
     r = build_fog_reference(a.force, a.reference_root)

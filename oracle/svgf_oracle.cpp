@@ -25,7 +25,7 @@
 // Parity status: the reference ships no tests, golden images or fixtures for
 // this path and its shader compiler (slangc) is absent, so the restatement is
 // pinned by (a) the reference shader source compiled as C++ through
-// oracle/build.py when /root/reference is present, and (b) closed-form
+// oracle/build.py when the reference checkout is present, and (b) closed-form
 // known-answer tests.  Without (a) the REF-EXACT half is "parity unpinned".
 //
 // Compile with -ffp-contract=off: the GPU path evaluates every threshold
@@ -319,6 +319,19 @@ struct FullParams {
     int32_t reserved;
 };
 
+// Stores of the FULL algorithm that the FP16 storage form rounds: the oracle
+// emulates each one separately, so that its share of the error against the
+// float64 result can be measured on its own.
+enum : int {
+    Q_INPUT = 1,   // radiance input rounded to binary16
+    Q_NORMAL = 2,  // guide normals as octahedral 2 x 16-bit codes
+    Q_TC = 4,      // temporally integrated colour (the level-0 input) in binary16
+    Q_HIST = 8,    // colour history in binary16
+    Q_MOM = 16,    // luminance moments in binary16
+    Q_RECORD = 32, // a-trous scratch records (colour, variance) in binary16
+    Q_OUTPUT = 64, // the denoised output in binary16
+};
+
 // Constants of the FULL algorithm (shared verbatim with the CUDA kernels).
 constexpr float kEpsL = 1e-4f;         // luminance edge-stop denominator floor
 constexpr float kEpsZ = 1e-3f;         // depth edge-stop denominator floor (metres)
@@ -367,8 +380,11 @@ template <class T> struct FullBuffers {
 template <class T>
 void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* depth, const T* normal3, const T* motion2,
                 const T* guide_prev, const T* hist_prev, const T* mom_prev, T* guide_cur, T* hist_cur, T* mom_cur,
-                T* out4, T* var_out, bool f16)
+                T* out4, T* var_out, int q)
 {
+    // Which stores of the FP16 storage form are emulated (a mask of the Q_* bits).
+    const bool q_in = q & Q_INPUT, q_nrm = q & Q_NORMAL, q_tc = q & Q_TC, q_hist = q & Q_HIST, q_mom = q & Q_MOM,
+               q_rec = q & Q_RECORD, q_out = q & Q_OUTPUT;
     const size_t n = size_t(w) * h;
     FullBuffers<T> B;
     B.tc.resize(4 * n);
@@ -385,8 +401,8 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
         for (int x = 0; x < w; ++x) {
             size_t i = size_t(y) * w + x;
             T nx = normal3[3 * i + 0], ny = normal3[3 * i + 1], nz = normal3[3 * i + 2];
-            T z = q32(depth[i], f16);
-            if (f16) oct16_roundtrip(nx, ny, nz);
+            T z = q32(depth[i], q_nrm);
+            if (q_nrm) oct16_roundtrip(nx, ny, nz);
             guide_cur[4 * i + 0] = nx;
             guide_cur[4 * i + 1] = ny;
             guide_cur[4 * i + 2] = nz;
@@ -406,7 +422,7 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
     for (int y = 0; y < h; ++y) {
         for (int x = 0; x < w; ++x) {
             size_t i = size_t(y) * w + x;
-            T cr = q16(radiance4[4 * i + 0], f16), cg = q16(radiance4[4 * i + 1], f16), cb = q16(radiance4[4 * i + 2], f16);
+            T cr = q16(radiance4[4 * i + 0], q_in), cg = q16(radiance4[4 * i + 1], q_in), cb = q16(radiance4[4 * i + 2], q_in);
             T nx = guide_cur[4 * i + 0], ny = guide_cur[4 * i + 1], nz = guide_cur[4 * i + 2], z = guide_cur[4 * i + 3];
             T gsum = std::fabs(B.gx[i]) + std::fabs(B.gy[i]);
             T ztol = T(kDepthRel) * z + T(kDepthGrad) * gsum + T(kDepthAbs);
@@ -482,12 +498,12 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                 mu = l;
                 var = T(0);
             }
-            B.tc[4 * i + 0] = q16(outr, f16);
-            B.tc[4 * i + 1] = q16(outg, f16);
-            B.tc[4 * i + 2] = q16(outb, f16);
+            B.tc[4 * i + 0] = q16(outr, q_tc);
+            B.tc[4 * i + 1] = q16(outg, q_tc);
+            B.tc[4 * i + 2] = q16(outb, q_tc);
             B.tc[4 * i + 3] = T(len);
-            mom_cur[2 * i + 0] = q16s(mu, f16);
-            mom_cur[2 * i + 1] = q16s(var, f16);
+            mom_cur[2 * i + 0] = q16s(mu, q_mom);
+            mom_cur[2 * i + 1] = q16s(var, q_mom);
         }
     }
 
@@ -501,7 +517,7 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
             T var;
             if (len < P.fallback_frames) {
                 T nx, ny, nz;
-                unit_normal(guide_cur + 4 * i, f16, nx, ny, nz);
+                unit_normal(guide_cur + 4 * i, q_nrm, nx, ny, nz);
                 T z = guide_cur[4 * i + 3];
                 T gx = B.gx[i], gy = B.gy[i];
                 T mup = mom_cur[2 * i + 0];
@@ -514,7 +530,7 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                         if (qx < 0 || qx >= w) continue;
                         size_t j = size_t(qy) * w + qx;
                         T qx_, qy_, qz_;
-                        unit_normal(guide_cur + 4 * j, f16, qx_, qy_, qz_);
+                        unit_normal(guide_cur + 4 * j, q_nrm, qx_, qy_, qz_);
                         T d = qx_ * nx + qy_ * ny + qz_ * nz;
                         T wn = normal_weight(d, P.sigma_n);
                         if (!(wn > T(0))) continue;
@@ -539,7 +555,7 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
             B.colA[4 * i + 0] = B.tc[4 * i + 0];
             B.colA[4 * i + 1] = B.tc[4 * i + 1];
             B.colA[4 * i + 2] = B.tc[4 * i + 2];
-            B.colA[4 * i + 3] = q16s(var, f16);
+            B.colA[4 * i + 3] = q16s(var, q_rec);
         }
     }
 
@@ -557,7 +573,7 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                 T cr = src[4 * i + 0], cg = src[4 * i + 1], cb = src[4 * i + 2], cv = src[4 * i + 3];
                 T cl = lum(cr, cg, cb);
                 T nx, ny, nz;
-                unit_normal(guide_cur + 4 * i, f16, nx, ny, nz);
+                unit_normal(guide_cur + 4 * i, q_nrm, nx, ny, nz);
                 T z = guide_cur[4 * i + 3];
                 T gx = B.gx[i], gy = B.gy[i];
                 // 3x3 Gaussian of the variance around the centre (inside taps only).
@@ -584,7 +600,7 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                         if (qx < 0 || qx >= w) continue;
                         size_t j = size_t(qy) * w + qx;
                         T ux, uy, uz;
-                        unit_normal(guide_cur + 4 * j, f16, ux, uy, uz);
+                        unit_normal(guide_cur + 4 * j, q_nrm, ux, uy, uz);
                         T d = ux * nx + uy * ny + uz * nz;
                         T wn = normal_weight(d, P.sigma_n);
                         if (!(wn > T(0))) continue;
@@ -615,22 +631,22 @@ void full_frame(const FullParams& P, int w, int h, const T* radiance4, const T* 
                     ov = cv;
                 }
                 if (lv == 0) {
-                    hist_cur[4 * i + 0] = q16(orr, f16);
-                    hist_cur[4 * i + 1] = q16(og, f16);
-                    hist_cur[4 * i + 2] = q16(ob, f16);
+                    hist_cur[4 * i + 0] = q16(orr, q_hist);
+                    hist_cur[4 * i + 1] = q16(og, q_hist);
+                    hist_cur[4 * i + 2] = q16(ob, q_hist);
                     hist_cur[4 * i + 3] = B.tc[4 * i + 3];
                 }
                 if (last) {
-                    out4[4 * i + 0] = q16(orr, f16);
-                    out4[4 * i + 1] = q16(og, f16);
-                    out4[4 * i + 2] = q16(ob, f16);
+                    out4[4 * i + 0] = q16(orr, q_out);
+                    out4[4 * i + 1] = q16(og, q_out);
+                    out4[4 * i + 2] = q16(ob, q_out);
                     out4[4 * i + 3] = T(1);
                     if (var_out) var_out[i] = ov;
                 } else {
-                    dst[4 * i + 0] = q16(orr, f16);
-                    dst[4 * i + 1] = q16(og, f16);
-                    dst[4 * i + 2] = q16(ob, f16);
-                    dst[4 * i + 3] = q16s(ov, f16);
+                    dst[4 * i + 0] = q16(orr, q_rec);
+                    dst[4 * i + 1] = q16(og, q_rec);
+                    dst[4 * i + 2] = q16(ob, q_rec);
+                    dst[4 * i + 3] = q16s(ov, q_rec);
                 }
             }
         }
@@ -683,7 +699,8 @@ int orc_ref_frame_f64(int w, int h, const double* raw, const double* mom_prev, d
 
 // FULL frame.  radiance: h*w*4, depth: h*w, normal: h*w*3, motion: h*w*2;
 // guide: h*w*4 (n.xyz, z), hist: h*w*4 (rgb, len), mom: h*w*2 (mu, var),
-// out: h*w*4, var_out: h*w or NULL.
+// out: h*w*4, var_out: h*w or NULL.  fp16_store: the Q_* mask of the stores
+// that are rounded as the FP16 storage form rounds them (0: none).
 int orc_full_frame_f32(const FullParams* p, int w, int h, const float* radiance, const float* depth,
                        const float* normal, const float* motion, const float* guide_prev, const float* hist_prev,
                        const float* mom_prev, float* guide_cur, float* hist_cur, float* mom_cur, float* out,
@@ -692,7 +709,7 @@ int orc_full_frame_f32(const FullParams* p, int w, int h, const float* radiance,
     if (!p || w <= 0 || h <= 0 || p->levels < 0 || p->levels > 12 || p->max_history < 1) return 1;
     Threads t(threads);
     full_frame<float>(*p, w, h, radiance, depth, normal, motion, guide_prev, hist_prev, mom_prev, guide_cur, hist_cur,
-                      mom_cur, out, var_out, fp16_store != 0);
+                      mom_cur, out, var_out, fp16_store);
     return 0;
 }
 
@@ -704,7 +721,7 @@ int orc_full_frame_f64(const FullParams* p, int w, int h, const double* radiance
     if (!p || w <= 0 || h <= 0 || p->levels < 0 || p->levels > 12 || p->max_history < 1) return 1;
     Threads t(threads);
     full_frame<double>(*p, w, h, radiance, depth, normal, motion, guide_prev, hist_prev, mom_prev, guide_cur, hist_cur,
-                       mom_cur, out, var_out, fp16_store != 0);
+                       mom_cur, out, var_out, fp16_store);
     return 0;
 }
 

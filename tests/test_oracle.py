@@ -242,6 +242,30 @@ def test_full_float32_agrees_with_float64():
         assert rel_l2(a, b) <= 1e-5
 
 
+def test_full_fp16_store_mask_decomposes():
+    """The FP16-storage emulation is a mask of independent stores: rounding only the radiance input equals feeding
+    binary16-rounded radiance with no emulation, the empty mask equals no emulation, and True rounds every store."""
+    from tron_grid_gb300 import scene
+
+    sc = scene.PlaneScene(scene.config1(64, 48, seed=7))
+    frames = [[sc.frame(t)[k].numpy() for k in ("radiance", "depth", "normal", "motion")] for t in range(4)]
+    states = {k: oracle.FullState(48, 64, np.float32) for k in ("in", "pre", "none", "zero", "all", "true")}
+    for rad, dep, nrm, mot in frames:
+        rad16 = rad.astype(np.float16).astype(np.float32)
+        a, _ = oracle.full_frame(P, states["in"], rad, dep, nrm, mot, fp16_store=oracle.Q_INPUT)
+        b, _ = oracle.full_frame(P, states["pre"], rad16, dep, nrm, mot, fp16_store=0)
+        np.testing.assert_array_equal(a, b)
+        c, _ = oracle.full_frame(P, states["none"], rad, dep, nrm, mot, fp16_store=False)
+        d, _ = oracle.full_frame(P, states["zero"], rad, dep, nrm, mot, fp16_store=0)
+        np.testing.assert_array_equal(c, d)
+        e, _ = oracle.full_frame(P, states["all"], rad, dep, nrm, mot, fp16_store=oracle.Q_ALL)
+        f, _ = oracle.full_frame(P, states["true"], rad, dep, nrm, mot, fp16_store=True)
+        np.testing.assert_array_equal(e, f)
+    # the storage form's mask leaves the records and (for an RGBA32F output) the output unrounded
+    assert oracle.fp16_storage_mask(False) & (oracle.Q_RECORD | oracle.Q_OUTPUT) == 0
+    assert oracle.fp16_storage_mask(True) & oracle.Q_OUTPUT
+
+
 def test_full_denoises():
     """On a static noisy scene without emitters the output is much closer to the truth than the input."""
     from tron_grid_gb300 import scene
