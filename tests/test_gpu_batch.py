@@ -111,10 +111,13 @@ def test_batch_fp16_against_oracle(cuda_dev):
             fr = seqs[j][t]
             nrm = oracle.oct16_decode(fr["normal"].cpu().numpy())
             ref, _ = oracle.full_frame(P, st[j], fr["radiance"].float().cpu().numpy(), fr["depth"].cpu().numpy(), nrm,
-                                       fr["motion"].cpu().numpy(), fp16_store=True)
+                                       fr["motion"].cpu().numpy(), fp16_store=oracle.fp16_storage_mask(True))
             g = outs[j].float().cpu().numpy()
+            # a last-place difference of an approximate SFU operation can flip one binary16 rounding of the
+            # history or the output, and a flipped history value persists through the EMA: agreement with the
+            # emulating oracle is bounded per pixel and, over the image, by one binary16 unit (2^-11)
             assert rel_err(g, ref).max() <= 2.0 ** -8
-            assert rel_l2(g, ref) <= 1e-4
+            assert rel_l2(g, ref) <= 2.0 ** -11
     b.close()
 
 

@@ -8,8 +8,11 @@ Tolerances
   exponential can move one stored value by one fp16 step, so the bound is 2
   fp16 units in the last place per value and 99.9% of values identical.
 * FULL with FP16 storage: against the float32 oracle with the same fp16 /
-  octahedral storage emulation (per-pixel 2^-8, mean 1e-5), and against the
-  float64 oracle without emulation: relative L2 luminance error <= 1e-3.
+  octahedral storage emulation (per-pixel 2^-8, mean 1e-4: a last-place
+  difference of an approximate SFU operation can flip one binary16 rounding of
+  the history, and the flip persists through the EMA), and against the
+  float64 oracle without emulation: relative L2 luminance error <= 1e-3
+  (test_gpu_full_size.py bounds every pixel against float64).
 """
 import numpy as np
 import pytest
@@ -57,7 +60,8 @@ def _run_full_pair(dev, spec, n_frames, storage=tg.STORAGE_FP32, fp16_inputs=Fal
         out = torch.empty((H, W, 4), dtype=out_dt, device=dev)
         den.denoise(rad_d, dep.to(dev), nrm_d, mot.to(dev), out=out)
         g = out.float().cpu().numpy()
-        r32, _ = oracle.full_frame(P, st32, rad_np, dep.numpy(), nrm_np, mot.numpy(), fp16_store=f16)
+        r32, _ = oracle.full_frame(P, st32, rad_np, dep.numpy(), nrm_np, mot.numpy(),
+                                   fp16_store=oracle.fp16_storage_mask(True) if f16 else 0)
         r64, _ = oracle.full_frame(P, st64, rad.numpy(), dep.numpy(), nrm.numpy(), mot.numpy(), fp16_store=False)
         results.append((g, r32, r64, fr))
         if check:
@@ -94,7 +98,7 @@ def _check_fp16(t, g, r32, r64):
     e = rel_err(g, r32)
     assert np.all(np.isfinite(g))
     assert e.max() <= 2.0 ** -8, f"frame {t}: max rel {e.max():.3e} vs emulating oracle"
-    assert e.mean() <= 1e-5, f"frame {t}: mean rel {e.mean():.3e} vs emulating oracle"
+    assert e.mean() <= 1e-4, f"frame {t}: mean rel {e.mean():.3e} vs emulating oracle"
     l2 = rel_l2(g, r64)
     assert l2 <= 1e-3, f"frame {t}: rel L2 vs float64 oracle {l2:.3e}"
 

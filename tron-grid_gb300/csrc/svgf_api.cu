@@ -109,8 +109,9 @@ static Layout layout_of(const tg_svgf_params& p)
     l.guide = f16 ? 8 : 16;
     l.c4 = f16 ? 8 : 16;
     l.mom = f16 ? 4 : 8;
-    // a-trous scratch: FULL records carry the guide (32 / 16 B), REF_EXACT images do not
-    l.rec = p.mode == TG_SVGF_MODE_FULL ? (f16 ? 16 : 32) : l.c4;
+    // a-trous scratch: FULL records carry the guide and stay float32 in both storage forms (32 B), REF_EXACT
+    // images are the reference's own formats
+    l.rec = p.mode == TG_SVGF_MODE_FULL ? 32 : l.c4;
     return l;
 }
 
@@ -148,8 +149,7 @@ size_t col_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
 {
     const size_t recs = col_var_offset_of(p, w, h);
     if (p.mode == TG_SVGF_MODE_REF_EXACT) return recs;
-    const size_t vb = p.storage == TG_SVGF_STORAGE_FP16 ? 2 : 4;
-    return recs + align_up(col_pixels_of(p, w, h) * vb, 256);
+    return recs + align_up(col_pixels_of(p, w, h) * sizeof(float), 256);
 }
 
 size_t fb_flags_bytes_of(uint32_t w, uint32_t h)
@@ -198,7 +198,7 @@ constexpr int kLevelR = 2;
 typedef void (*LevelTmaFn)(FullArgs, LevelArgs, LevelGeom, const CUtensorMap, const CUtensorMap);
 typedef void (*LevelTiledFn)(FullArgs, LevelGeom);
 
-// The FULL a-trous kernel for a level: FP16 or FP32 records, VAR = false at the
+// The FULL a-trous kernel for a level: FP16 or FP32 storage, VAR = false at the
 // last level (it writes only colour), PL at level 0 (staged from the planes).
 template <bool PL> LevelTmaFn level_tma_kernel(bool f16, bool last)
 {
@@ -338,9 +338,8 @@ EncodeTiledFn encode_tiled()
 }
 
 // One tensor map per a-trous level L >= 1 over that level's input records in
-// the residue-major layout of stride 2^L: FP32 {float, row, plane, half-plane},
-// FP16 {8-byte element (two per record), row, plane}; box = one 36 x 20 halo
-// tile, whose rows are contiguous lines.
+// the residue-major layout of stride 2^L: {float, row, plane, half-plane};
+// box = one 36 x 20 halo tile, whose rows are contiguous lines.
 // Level 0 has no records: its maps cover the tc and guide planes.
 void build_tensor_maps(tg_svgf* s)
 {
@@ -353,26 +352,14 @@ void build_tensor_maps(tg_svgf* s)
         const ResLayout L = res_layout(int(s->w), int(s->h), lv);
         void* base = (lv & 1) ? s->colB : s->colA;
         const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
-        CUresult r;
-        if (f16) {
-            // a row of 16-byte records as 2 pw 8-byte elements: one contiguous 576-byte line per tile row
-            const cuuint64_t dim[3] = {2ull * L.pw, cuuint64_t(L.ph), planes};
-            const cuuint64_t str[2] = {16ull * L.pw, 16ull * L.pw * L.ph};
-            const cuuint32_t box[3] = {2 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1};
-            const cuuint32_t es[3] = {1, 1, 1};
-            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, dim, str, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        } else {
-            // a row of either half-plane as 4 pw floats: one contiguous 576-byte line per tile row and half
-            const cuuint64_t dim[4] = {4ull * L.pw, cuuint64_t(L.ph), planes, 2};
-            const cuuint64_t str[3] = {16ull * L.pw, 16ull * L.pw * L.ph, 16ull * col_guide_half_of(s->p, s->w, s->h)};
-            const cuuint32_t box[4] = {4 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1, 1};
-            const cuuint32_t es[4] = {1, 1, 1, 1};
-            r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dim, str, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        }
+        // a row of either half-plane as 4 pw floats: one contiguous 576-byte line per tile row and half
+        const cuuint64_t dim[4] = {4ull * L.pw, cuuint64_t(L.ph), planes, 2};
+        const cuuint64_t str[3] = {16ull * L.pw, 16ull * L.pw * L.ph, 16ull * col_guide_half_of(s->p, s->w, s->h)};
+        const cuuint32_t box[4] = {4 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1, 1};
+        const cuuint32_t es[4] = {1, 1, 1, 1};
+        const CUresult r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dim, str, box, es,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return;
     }
     s->tma = true;
@@ -591,8 +578,8 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         const double inb = fmt_bytes(in->radiance.format) + fmt_bytes(in->depth.format) +
                            fmt_bytes(in->normal.format) + fmt_bytes(in->motion.format);
         const double ob = fmt_bytes(out->denoised.format);
-        const double vb = f16 ? 2 : 4;    // variance plane entry
-        const double rb = f16 ? 16 : 32;  // a-trous record
+        const double vb = 4;   // variance plane entry
+        const double rb = 32;  // a-trous record
         // temporal: inputs + previous guide/history/moments, writes guide, tc, moments, depth gradient and
         // the variance plane entry (every pixel with a history of fallback_frames or more)
         launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm) + 8 + vb), [&] {

@@ -100,14 +100,14 @@ __device__ __forceinline__ int find_stream(const int* pf, int n, int item)
 // The persistent kernel runs the pixel stages on its level-shaped CTAs, and
 // K2 stages its tile in the level tile's shared memory.
 static_assert(kLvTX == kBlockX && kLvRows == kBlockY, "pixel and level CTAs must have the same shape");
-static_assert(sizeof(VarTile) <= sizeof(LevelSmem<1, ST_FP32>), "K2 tile must fit the level tile");
+static_assert(sizeof(VarTile) <= sizeof(LevelSmem<1>), "K2 tile must fit the level tile");
 
 template <int ST, int R>
 __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __restrict__ table, int cap,
                                                                    BarrierState* bar, unsigned expect_blocks,
                                                                    long long spin_cycles)
 {
-    __shared__ LevelSmem<R, ST> sm;
+    __shared__ LevelSmem<R> sm;
     __shared__ VarList vl;
     const BatchHeader hd = *reinterpret_cast<const BatchHeader*>(table);
     const int* prefix = reinterpret_cast<const int*>(table + table_prefix_offset());
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kBlockX* kBlockY) k_ms_pixel(const char* __res
 template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level(const char* __restrict__ table, int cap, int L)
 {
-    __shared__ LevelSmem<R, ST> sm;
+    __shared__ LevelSmem<R> sm;
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
     const int item = blockIdx.x;

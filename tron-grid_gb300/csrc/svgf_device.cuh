@@ -267,6 +267,9 @@ template <> struct Stor<ST_FP32> {
     __device__ static float4 ld_guide_w(const guide_t* p, size_t i) { return __ldg(p + i); }
     __device__ static float ld_guide_z(const guide_t* p, size_t i) { return __ldg(reinterpret_cast<const float*>(p + i) + 3); }
     __device__ static guide_t mk_guide(float3 n, uint32_t, float z) { return make_float4(n.x, n.y, n.z, z); }
+    // the guide as stored (FP32: unit normal and depth)
+    typedef float4 graw_t;
+    __device__ static graw_t ld_graw(const guide_t* p, size_t i) { return __ldg(p + i); }
     __device__ static float4 ld4(const c4_t* p, size_t i) { return __ldg(p + i); }
     __device__ static float ld4_w(const c4_t* p, size_t i) { return __ldg(reinterpret_cast<const float*>(p + i) + 3); }
     __device__ static void st4(c4_t* p, size_t i, float4 v) { p[i] = v; }
@@ -277,34 +280,6 @@ template <> struct Stor<ST_FP32> {
     __device__ static float4 rt4(float4 v) { return v; }
     __device__ static float2 rtm(float2 v) { return v; }
     __device__ static float qin(float v) { return v; }
-    // a-trous scratch record (32 B): float4 (r, g, b, var) in the colour half-plane at i, the guide float4
-    // (n, z) in the guide half-plane at gh + i; a tile row of either half is one contiguous run
-    typedef float4 rec_t;
-    typedef float4 graw_t;
-    static constexpr int kRecBytes = 32;
-    __device__ static graw_t ld_graw(const guide_t* p, size_t i) { return __ldg(p + i); }
-    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g, size_t gh)
-    {
-        c = __ldg(p + i);
-        g = __ldg(p + gh + i);
-    }
-    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g, size_t gh)
-    {
-        p[i] = c;
-        p[gh + i] = g;
-    }
-    // variance plane beside the records (`off` bytes after the buffer start), 4 B per record
-    typedef float var_t;
-    __device__ static const var_t* var_ptr(const void* buf, size_t off)
-    {
-        return reinterpret_cast<const float*>(static_cast<const char*>(buf) + off);
-    }
-    __device__ static float var_at(const var_t* p, int i) { return __ldg(p + i); }
-    __device__ static float ld_var(const void* buf, size_t off, size_t i) { return __ldg(var_ptr(buf, off) + i); }
-    __device__ static void st_var(void* buf, size_t off, size_t i, float v)
-    {
-        reinterpret_cast<float*>(static_cast<char*>(buf) + off)[i] = v;
-    }
 };
 
 template <> struct Stor<ST_FP16> {
@@ -330,6 +305,9 @@ template <> struct Stor<ST_FP16> {
         return __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(p + i) + 1));
     }
     __device__ static guide_t mk_guide(float3, uint32_t enc, float z) { return make_uint2(enc, __float_as_uint(z)); }
+    // the guide as stored (FP16 storage: octahedral code and depth bits)
+    typedef uint2 graw_t;
+    __device__ static graw_t ld_graw(const guide_t* p, size_t i) { return __ldg(p + i); }
     __device__ static float4 ld4(const c4_t* p, size_t i) { return unpack_h4(__ldg(p + i)); }
     __device__ static float ld4_w(const c4_t* p, size_t i)
     {
@@ -347,37 +325,37 @@ template <> struct Stor<ST_FP16> {
     __device__ static float4 rt4(float4 v) { return unpack_h4(pack_h4(v)); }
     __device__ static float2 rtm(float2 v) { return unpack_h2(pack_h2(sat16(v.x), sat16(v.y))); }
     __device__ static float qin(float v) { return q16(v); }
-    // a-trous scratch record (16 B): half (r, g), half (b, var), octahedral code, z bits
-    typedef uint4 rec_t;
-    typedef uint2 graw_t;
-    static constexpr int kRecBytes = 16;
-    __device__ static graw_t ld_graw(const guide_t* p, size_t i) { return __ldg(p + i); }
-    __device__ static void decode_rec(uint4 u, float4& c, float4& g)
+};
+
+// A-trous scratch records, the same for both storage forms (binary16 records
+// were the largest error term of the FP16 form against float64, so the
+// scratch stays float32): float4 (r, g, b, var) in the colour half-plane at i,
+// the guide float4 (unit normal, z) in the guide half-plane at gh + i; a tile
+// row of either half is one contiguous run.  Beside the records, a plane of
+// their variances (`off` bytes after the buffer start), 4 B per record.
+struct Rec {
+    typedef float4 rec_t;
+    static constexpr int kRecBytes = 32;
+    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g, size_t gh)
     {
-        const float2 a = unpack_h2(u.x), b = unpack_h2(u.y);
-        c = make_float4(a.x, a.y, b.x, b.y);
-        const float3 n = oct16_decode_fast(u.z);
-        g = make_float4(n.x, n.y, n.z, __uint_as_float(u.w));
+        c = __ldg(p + i);
+        g = __ldg(p + gh + i);
     }
-    __device__ static void ld_rec(const rec_t* p, size_t i, float4& c, float4& g, size_t)
+    __device__ static void st_rec(rec_t* p, size_t i, float4 c, float4 g, size_t gh)
     {
-        decode_rec(__ldg(p + i), c, g);
+        p[i] = c;
+        p[gh + i] = g;
     }
-    __device__ static void st_rec(rec_t* p, size_t i, float4 c, graw_t g, size_t)
-    {
-        p[i] = make_uint4(pack_h2(c.x, c.y), pack_h2(c.z, sat16(c.w)), g.x, g.y);
-    }
-    // variance plane beside the records, 2 B per record: the same half as the record's
-    typedef unsigned short var_t;
+    typedef float var_t;
     __device__ static const var_t* var_ptr(const void* buf, size_t off)
     {
-        return reinterpret_cast<const unsigned short*>(static_cast<const char*>(buf) + off);
+        return reinterpret_cast<const float*>(static_cast<const char*>(buf) + off);
     }
-    __device__ static float var_at(const var_t* p, int i) { return __half2float(__ushort_as_half(__ldg(p + i))); }
-    __device__ static float ld_var(const void* buf, size_t off, size_t i) { return var_at(var_ptr(buf, off), int(i)); }
+    __device__ static float var_at(const var_t* p, int i) { return __ldg(p + i); }
+    __device__ static float ld_var(const void* buf, size_t off, size_t i) { return __ldg(var_ptr(buf, off) + i); }
     __device__ static void st_var(void* buf, size_t off, size_t i, float v)
     {
-        reinterpret_cast<unsigned short*>(static_cast<char*>(buf) + off)[i] = __half_as_ushort(__float2half_rn(sat16(v)));
+        reinterpret_cast<float*>(static_cast<char*>(buf) + off)[i] = v;
     }
 };
 

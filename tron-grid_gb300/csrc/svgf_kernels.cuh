@@ -242,7 +242,7 @@ template <int ST> __device__ __forceinline__ bool full_temporal_px(const FullArg
     S::stm(static_cast<M*>(a.mom_cur), i, mom);
     const float4 t = S::rt4(tcv);
     if (int(t.w) < a.fallback_frames) return true;
-    S::st_var(a.col_dst, a.var_off, i, S::rtm(mom).y);
+    Rec::st_var(a.col_dst, a.var_off, i, S::rtm(mom).y);
     return false;
 }
 
@@ -313,7 +313,7 @@ __device__ __forceinline__ void full_variance_px(const FullArgs& a, int x, int y
         const float m1 = s1 / s0;
         var = fmaxf(0.0f, s2 / s0 - m1 * m1);
     }
-    S::st_var(a.col_dst, a.var_off, i, var);
+    Rec::st_var(a.col_dst, a.var_off, i, var);
 }
 
 // One kBlockX x kBlockY pixel block `blk` (row-major over the image's blocks)

@@ -68,20 +68,12 @@ template <int R> struct LevelOcc {
 };
 
 // Staged tile of one level: X0 = (r, g, b, variance), X1 = (unit normal, depth),
-// XL = luminance; FP16 storage also keeps each record's octahedral normal code
-// (XO), which the output record carries on unchanged.  X0 and X1 are 128-byte
-// aligned so that a TMA box can land in them directly (N * 16 bytes is a
-// multiple of 128 for every tile shape used).
-template <int R, int ST> struct __align__(128) LevelSmem {
+// XL = luminance.  X0 and X1 are 128-byte aligned so that a TMA box can land in
+// them directly (N * 16 bytes is a multiple of 128 for every tile shape used).
+template <int R> struct __align__(128) LevelSmem {
     float4 X0[LevelTile<R>::N];
     float4 X1[LevelTile<R>::N];
     float XL[LevelTile<R>::N];
-};
-template <int R> struct __align__(128) LevelSmem<R, ST_FP16> {
-    float4 X0[LevelTile<R>::N];
-    float4 X1[LevelTile<R>::N];
-    float XL[LevelTile<R>::N];
-    uint32_t XO[LevelTile<R>::N];
 };
 
 // Maps tile `bid` to (residue a, b) and its tile origin in sub-lattice units.
@@ -164,7 +156,7 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
         const int t = rb + f - 1;
         rowf[f] = ((t & m) << lg) * P + (t >> lg) * pw + j_base;
     }
-    const typename S::var_t* vp = S::var_ptr(lv.col_src, lv.var_off);
+    const Rec::var_t* vp = Rec::var_ptr(lv.col_src, lv.var_off);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int y = rb + s * (j0 + int(threadIdx.y) * R + k);
@@ -175,7 +167,7 @@ __device__ __forceinline__ void level_prefetch(const FullArgs& a, const LevelArg
             const bool oy = pre.valid[k] && (IN || unsigned(y + f - 1) < unsigned(a.h));
 #pragma unroll
             for (int e = 0; e < 3; ++e)
-                pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? S::var_at(vp, rowf[f] + k * pw + cxo[e]) : 0.f;
+                pre.vn9[k][f * 3 + e] = (oy && cxv[e]) ? Rec::var_at(vp, rowf[f] + k * pw + cxo[e]) : 0.f;
         }
     }
 }
@@ -206,7 +198,7 @@ __device__ __forceinline__ bool tile_interior(const FullArgs& a, int s, int ra, 
 template <int ST, int R, bool VAR, bool IN>
 __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra,
                                               int rb, int i0, int j0, const CentrePre<ST, R>& pre,
-                                              const LevelSmem<R, ST>& sm)
+                                              const LevelSmem<R>& sm)
 {
     typedef Stor<ST> S;
     typedef typename S::c4_t C4;
@@ -319,39 +311,31 @@ __device__ __forceinline__ void level_compute(const FullArgs& a, const LevelArgs
         }
         if (lv.level == 0) S::st4(static_cast<C4*>(a.hist_cur), i, make_float4(o.x, o.y, o.z, len[k]));
         if (lv.last) {
-            st_rgba(a.out, cx, y, make_float4(S::qin(o.x), S::qin(o.y), S::qin(o.z), 1.0f));
+            st_rgba(a.out, cx, y, make_float4(o.x, o.y, o.z, 1.0f));
         } else {
-            typename S::graw_t graw;
-            if constexpr (ST == ST_FP16)
-                graw = make_uint2(sm.XO[c], __float_as_uint(sm.X1[c].w));
-            else
-                graw = sm.X1[c];
             const size_t oi = res_idx(lv.lout, cx, y);
-            S::st_rec(static_cast<typename S::rec_t*>(lv.col_dst), oi, o, graw, lv.ghalf);
-            S::st_var(lv.col_dst, lv.var_off, oi, o.w);
+            Rec::st_rec(static_cast<Rec::rec_t*>(lv.col_dst), oi, o, sm.X1[c], lv.ghalf);
+            Rec::st_var(lv.col_dst, lv.var_off, oi, o.w);
         }
     }
 }
 
 // Level 0 reads the planes K1 writes instead of records: the staged cell's
 // colour from tc, its variance from the variance plane, its guide from
-// guide_cur (FP16: the octahedral code too).  Every FULL path stages level 0
-// this way (PL); K1 and K2 write no level-0 records.
+// guide_cur (FP16 storage: decoded from the octahedral code).  Every FULL path
+// stages level 0 this way (PL); K1 and K2 write no level-0 records.
 template <int ST>
-__device__ __forceinline__ void plane_cell(const FullArgs& a, const LevelArgs& lv, size_t j, float4& c, float4& n,
-                                           uint32_t& oct)
+__device__ __forceinline__ void plane_cell(const FullArgs& a, const LevelArgs& lv, size_t j, float4& c, float4& n)
 {
     typedef Stor<ST> S;
     const float4 t = S::ld4(static_cast<const typename S::c4_t*>(a.tc), j);
-    c = make_float4(t.x, t.y, t.z, S::ld_var(lv.col_src, lv.var_off, j));
+    c = make_float4(t.x, t.y, t.z, Rec::ld_var(lv.col_src, lv.var_off, j));
     if constexpr (ST == ST_FP16) {
         const uint2 u = S::ld_graw(static_cast<const typename S::guide_t*>(a.guide_cur), j);
         const float3 v = oct16_decode_fast(u.x);
         n = make_float4(v.x, v.y, v.z, __uint_as_float(u.y));
-        oct = u.x;
     } else {
         n = S::ld_graw(static_cast<const typename S::guide_t*>(a.guide_cur), j);
-        oct = 0;
     }
 }
 
@@ -360,34 +344,25 @@ __device__ __forceinline__ void plane_cell(const FullArgs& a, const LevelArgs& l
 // caller synchronises the CTA before reusing `sm`.
 template <int ST, int R, bool VAR, bool PL, bool IN>
 __device__ __forceinline__ void level_tile_body(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra,
-                                                int rb, int i0, int j0, LevelSmem<R, ST>& sm)
+                                                int rb, int i0, int j0, LevelSmem<R>& sm)
 {
-    typedef Stor<ST> S;
-    typedef typename S::rec_t RT;
     typedef LevelTile<R> T;
     const int s = g.s;
     CentrePre<ST, R> pre;
     level_prefetch<ST, R, IN>(a, lv, s, ra, rb, i0, j0, pre);
-    const RT* src = static_cast<const RT*>(lv.col_src);
+    const Rec::rec_t* src = static_cast<const Rec::rec_t*>(lv.col_src);
     const int pw = lv.lin.pw, P = lv.lin.pw * lv.lin.ph;
     const int plane = ((rb << lv.lin.lg) + ra) * P;
     for (int k = threadIdx.y * kLvTX + threadIdx.x; k < T::N; k += kLvTX * kLvRows) {
         float4 c = make_float4(0.f, 0.f, 0.f, 0.f), n = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint32_t oct = 0;
         if (IN || staged_inside<R>(a, s, ra, rb, i0, j0, k)) {
             const int sj = k / T::SW, si = k - sj * T::SW;
             const size_t ri = plane + (j0 + sj - 2) * pw + (i0 + si - 2);
-            if constexpr (PL) {
-                plane_cell<ST>(a, lv, ri, c, n, oct);
-            } else if constexpr (ST == ST_FP16) {
-                const uint4 u = __ldg(src + ri);
-                S::decode_rec(u, c, n);
-                oct = u.z;
-            } else {
-                S::ld_rec(src, ri, c, n, lv.ghalf);
-            }
+            if constexpr (PL)
+                plane_cell<ST>(a, lv, ri, c, n);
+            else
+                Rec::ld_rec(src, ri, c, n, lv.ghalf);
         }
-        if constexpr (ST == ST_FP16) sm.XO[k] = oct;
         sm.X0[k] = c;
         sm.X1[k] = n;
         sm.XL[k] = lum(c.x, c.y, c.z);
@@ -398,7 +373,7 @@ __device__ __forceinline__ void level_tile_body(const FullArgs& a, const LevelAr
 
 template <int ST, int R, bool VAR = true, bool PL = false>
 __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
-                                                LevelSmem<R, ST>& sm)
+                                                LevelSmem<R>& sm)
 {
     int ra, rb, i0, j0;
     level_block(g, bid, LevelTile<R>::TX, LevelTile<R>::TY, ra, rb, i0, j0);
@@ -411,7 +386,7 @@ __device__ __forceinline__ void full_level_tile(const FullArgs& a, const LevelAr
 template <int ST, int R, bool VAR, bool PL = false>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
-    __shared__ LevelSmem<R, ST> sm;
+    __shared__ LevelSmem<R> sm;
     full_level_tile<ST, R, VAR, PL>(a, level_args_of(a), g, blockIdx.x, sm);
 }
 
@@ -419,13 +394,13 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_lev
 //
 // The same level with the halo tile staged by the tensor-memory accelerator:
 // one elected thread issues cp.async.bulk.tensor for the tile's box of
-// residue-major records (FP32: 4-D map {float, row, plane, half-plane}, so that
-// the box of each half lands as one dense float4 array and each tile row is one
-// contiguous 576-byte line; FP16: a 3-D map {8-byte element, row, plane}, each
-// tile row of 16-byte records one 576-byte line), completion is
-// tracked by an mbarrier transaction count, and cells outside the plane array
-// arrive zero-filled.  The wait is bounded: a box that has not landed after
-// about a second sets a->err and the CTA returns.
+// residue-major records (a 4-D map {float, row, plane, half-plane}, so that the
+// box of each half lands as one dense float4 array and each tile row is one
+// contiguous 576-byte line); level 0 reads two 2-D maps over the tc and guide
+// planes instead.  Completion is tracked by an mbarrier transaction count and
+// cells outside the plane array arrive zero-filled.  The wait is bounded: a box
+// that has not landed after about a second sets a->err, the CTA waits (bounded)
+// once more for the copy to retire, and returns.
 
 constexpr long long kTmaWaitCycles = 2000000000LL;
 
@@ -445,25 +420,64 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase)
     }
 }
 
-// Landing area of level 0's two FP16 plane boxes (8-byte tc and guide texels),
-// which cannot be decoded in place; other instantiations use an empty one.
-template <int R> struct __align__(128) PlaneRaw16 {
-    uint2 c[LevelTile<R>::N];
-    uint2 g[LevelTile<R>::N];
-};
-struct NoRaw {};
+// Issues the halo box of the tile at (ra, rb, i0, j0) into `sm` (one thread).
+// Level 0 with FP16 storage lands its two 8-byte-texel boxes in X1 (tc in the
+// first N * 8 bytes, the guide in the next), to be decoded into X0 / X1.
+template <int ST, int R, bool PL>
+__device__ __forceinline__ void tma_issue(const LevelGeom& g, int ra, int rb, int i0, int j0, LevelSmem<R>& sm,
+                                          uint32_t ubar, const CUtensorMap* tm, const CUtensorMap* tm2)
+{
+    typedef LevelTile<R> T;
+    const uint64_t map = reinterpret_cast<uint64_t>(tm);
+    if constexpr (PL) {
+        const uint64_t map2 = reinterpret_cast<uint64_t>(tm2);
+        const uint32_t bytes = 2u * T::N * (ST == ST_FP16 ? 8u : 16u);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
+        if constexpr (ST == ST_FP16) {
+            // 8-byte texels: x = i0 - 2 texels is even (i0 is a multiple of 32), so the box starts on 16 bytes
+            const uint32_t d = smem_u32(sm.X1);
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                asm volatile(
+                    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                    "[%4];" ::"r"(d + h * T::N * 8u),
+                    "l"(h == 0 ? map : map2), "r"(i0 - 2), "r"(j0 - 2), "r"(ubar)
+                    : "memory");
+        } else {
+            // x = 4 (i0 - 2) floats: the box starts on a 16-byte boundary
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                asm volatile(
+                    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                    "[%4];" ::"r"(smem_u32(h == 0 ? sm.X0 : sm.X1)),
+                    "l"(h == 0 ? map : map2), "r"(4 * (i0 - 2)), "r"(j0 - 2), "r"(ubar)
+                    : "memory");
+        }
+    } else {
+        const int plane = (rb << g.lg) + ra;
+        const uint32_t bytes = 2u * T::N * 16u;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
+        // x = 4 (i0 - 2) floats: the box starts on a 16-byte boundary
+#pragma unroll
+        for (int half = 0; half < 2; ++half)
+            asm volatile(
+                "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+                "[%6];" ::"r"(smem_u32(half == 0 ? sm.X0 : sm.X1)),
+                "l"(map), "r"(4 * (i0 - 2)), "r"(j0 - 2), "r"(plane), "r"(half), "r"(ubar)
+                : "memory");
+    }
+}
 
 // The TMA kernel after its copy is issued: prefetch, bounded wait, fix-up,
 // compute.  IN: the tile is interior (tile_interior), so no cell needs a test.
-template <int ST, int R, bool VAR, bool PL, bool IN, class Raw16>
+template <int ST, int R, bool VAR, bool PL, bool IN>
 __device__ __forceinline__ void tma_tile_body(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int ra, int rb,
-                                              int i0, int j0, int tid, uint32_t ubar, LevelSmem<R, ST>& sm,
-                                              const Raw16& raw16)
+                                              int i0, int j0, int tid, uint32_t ubar, LevelSmem<R>& sm)
 {
     typedef LevelTile<R> T;
-    constexpr int kCells = (T::N + kLvTX * kLvRows - 1) / (kLvTX * kLvRows);
+    constexpr int kThreads = kLvTX * kLvRows;
+    constexpr int kCells = (T::N + kThreads - 1) / kThreads;
     const int s = g.s;
-    const uint4* raw = reinterpret_cast<const uint4*>(sm.X1);
     CentrePre<ST, R> pre;
     level_prefetch<ST, R, IN>(a, lv, s, ra, rb, i0, j0, pre);
     // PL: the staged cells' variances (the plane is row-major at level 0)
@@ -471,11 +485,11 @@ __device__ __forceinline__ void tma_tile_body(const FullArgs& a, const LevelArgs
     if constexpr (PL) {
 #pragma unroll
         for (int e = 0; e < kCells; ++e) {
-            const int k = tid + e * kLvTX * kLvRows;
+            const int k = tid + e * kThreads;
             cv[e] = 0.f;
             if (k < T::N && (IN || staged_inside<R>(a, s, ra, rb, i0, j0, k))) {
                 const int sj = k / T::SW, si = k - sj * T::SW;
-                cv[e] = Stor<ST>::ld_var(lv.col_src, lv.var_off, size_t(j0 + sj - 2) * a.w + (i0 + si - 2));
+                cv[e] = Rec::ld_var(lv.col_src, lv.var_off, size_t(j0 + sj - 2) * a.w + (i0 + si - 2));
             }
         }
     }
@@ -487,36 +501,51 @@ __device__ __forceinline__ void tma_tile_body(const FullArgs& a, const LevelArgs
         }
         return;
     }
-    // Zero the cells outside the image, compute luminance (and decode FP16 records).
+    if constexpr (PL && ST == ST_FP16) {
+        // the raw texels of this thread's cells, read before any thread overwrites X1 with decoded guides
+        const uint2* rc = reinterpret_cast<const uint2*>(sm.X1);
+        const uint2* rg = rc + T::N;
+        uint2 tc[kCells], gd[kCells];
 #pragma unroll
-    for (int e = 0; e < kCells; ++e) {
-        const int k = tid + e * kLvTX * kLvRows;
-        if (k >= T::N) break;
-        const bool in = IN || staged_inside<R>(a, s, ra, rb, i0, j0, k);
-        float4 c, n;
-        if constexpr (PL && ST == ST_FP16) {
-            const float4 t = unpack_h4(raw16.c[k]);
-            const uint2 u = raw16.g[k];
-            const float3 v = oct16_decode_fast(u.x);
-            c = make_float4(t.x, t.y, t.z, cv[e]);
-            n = make_float4(v.x, v.y, v.z, __uint_as_float(u.y));
-            sm.XO[k] = u.x;
-        } else if constexpr (ST == ST_FP16) {
-            const uint4 u = raw[k];
-            Stor<ST_FP16>::decode_rec(u, c, n);
-            sm.XO[k] = u.z;
-        } else {
-            c = sm.X0[k];
-            n = sm.X1[k];
+        for (int e = 0; e < kCells; ++e) {
+            const int k = tid + e * kThreads;
+            tc[e] = k < T::N ? rc[k] : make_uint2(0u, 0u);
+            gd[e] = k < T::N ? rg[k] : make_uint2(0u, 0u);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < kCells; ++e) {
+            const int k = tid + e * kThreads;
+            if (k >= T::N) break;
+            const bool in = IN || staged_inside<R>(a, s, ra, rb, i0, j0, k);
+            const float4 t = unpack_h4(tc[e]);
+            const float3 v = oct16_decode_fast(gd[e].x);
+            float4 c = make_float4(t.x, t.y, t.z, cv[e]);
+            float4 n = make_float4(v.x, v.y, v.z, __uint_as_float(gd[e].y));
+            if (!in) {
+                c = make_float4(0.f, 0.f, 0.f, 0.f);
+                n = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            sm.X0[k] = c;
+            sm.X1[k] = n;
+            sm.XL[k] = lum(c.x, c.y, c.z);
+        }
+    } else {
+        // zero the cells outside the image, compute luminance
+#pragma unroll
+        for (int e = 0; e < kCells; ++e) {
+            const int k = tid + e * kThreads;
+            if (k >= T::N) break;
+            const bool in = IN || staged_inside<R>(a, s, ra, rb, i0, j0, k);
+            float4 c = sm.X0[k];
             if constexpr (PL) c.w = cv[e];
+            if (!in) {
+                c = make_float4(0.f, 0.f, 0.f, 0.f);
+                sm.X1[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            if (PL || !in) sm.X0[k] = c;
+            sm.XL[k] = lum(c.x, c.y, c.z);
         }
-        if (!in) {
-            c = make_float4(0.f, 0.f, 0.f, 0.f);
-            n = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        if (ST == ST_FP16 || PL || !in) sm.X0[k] = c;
-        if (ST == ST_FP16 || !in) sm.X1[k] = n;
-        sm.XL[k] = lum(c.x, c.y, c.z);
     }
     __syncthreads();
     level_compute<ST, R, VAR, IN>(a, lv, g, ra, rb, i0, j0, pre, sm);
@@ -524,26 +553,19 @@ __device__ __forceinline__ void tma_tile_body(const FullArgs& a, const LevelArgs
 
 // One level with its tile staged by TMA.  VAR = false at the last level (colour
 // only).  PL (level 0): the box comes from two row-major images instead of the
-// records, tc through `tm` and guide_cur through `tm2` (FP32: 2-D maps
-// {float, row} landing as X0 and X1; FP16: 2-D maps of 8-byte texels landing
-// in PlaneRaw16), and each staged cell's variance comes from the variance
-// plane, loaded before the wait.  Other levels read `tm` only.
+// records, tc through `tm` and guide_cur through `tm2`, and each staged cell's
+// variance comes from the variance plane, loaded before the wait.  Other levels
+// read `tm` only.
 template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
     k_full_level_tma(FullArgs a, LevelArgs lv, LevelGeom g, const __grid_constant__ CUtensorMap tm,
                      const __grid_constant__ CUtensorMap tm2)
 {
     typedef LevelTile<R> T;
-    typedef typename std::conditional<PL && ST == ST_FP16, PlaneRaw16<R>, NoRaw>::type Raw16;
-    __shared__ LevelSmem<R, ST> sm;
-    __shared__ Raw16 raw16;
+    __shared__ LevelSmem<R> sm;
     __shared__ __align__(8) uint64_t bar;
-    // FP16 records (16 B) land in the X1 array and are decoded in place: each
-    // thread reads raw record k before it writes X0/X1/XL entry k.
-    uint4* raw = reinterpret_cast<uint4*>(sm.X1);
     int ra, rb, i0, j0;
     level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
-    const int s = g.s;
     const int tid = threadIdx.y * kLvTX + threadIdx.x;
     const uint32_t ubar = smem_u32(&bar);
     if (tid == 0) {
@@ -552,59 +574,11 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
-    const int plane = (rb << lv.lin.lg) + ra;
-    if (tid == 0) {
-        const uint64_t map = reinterpret_cast<uint64_t>(&tm);
-        if constexpr (PL) {
-            const uint64_t map2 = reinterpret_cast<uint64_t>(&tm2);
-            const uint32_t bytes = 2u * T::N * (ST == ST_FP16 ? 8u : 16u);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
-            if constexpr (ST == ST_FP16) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
-                    asm volatile(
-                        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-                        "[%4];" ::"r"(smem_u32(h == 0 ? raw16.c : raw16.g)),
-                        "l"(h == 0 ? map : map2), "r"(i0 - 2), "r"(j0 - 2), "r"(ubar)
-                        : "memory");
-            } else {
-                // x = 4 (i0 - 2) floats: the box starts on a 16-byte boundary
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
-                    asm volatile(
-                        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-                        "[%4];" ::"r"(smem_u32(h == 0 ? sm.X0 : sm.X1)),
-                        "l"(h == 0 ? map : map2), "r"(4 * (i0 - 2)), "r"(j0 - 2), "r"(ubar)
-                        : "memory");
-            }
-        } else if constexpr (ST == ST_FP32) {
-            // x = 4 (i0 - 2) floats: the box starts on a 16-byte boundary
-            const uint32_t bytes = 2u * T::N * 16u;
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const uint32_t dst = smem_u32(half == 0 ? sm.X0 : sm.X1);
-                asm volatile(
-                    "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-                    "[%6];" ::"r"(dst),
-                    "l"(map), "r"(4 * (i0 - 2)), "r"(j0 - 2), "r"(plane), "r"(half), "r"(ubar)
-                    : "memory");
-            }
-        } else {
-            // rows of 8-byte elements, two per record: x = 2 (i0 - 2) is even, so the box starts on 16 bytes
-            const uint32_t bytes = T::N * 16u;
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
-            asm volatile(
-                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-                "[%5];" ::"r"(smem_u32(raw)),
-                "l"(map), "r"(2 * (i0 - 2)), "r"(j0 - 2), "r"(plane), "r"(ubar)
-                : "memory");
-        }
-    }
-    if (tile_interior<R>(a, s, ra, rb, i0, j0))
-        tma_tile_body<ST, R, VAR, PL, true>(a, lv, g, ra, rb, i0, j0, tid, ubar, sm, raw16);
+    if (tid == 0) tma_issue<ST, R, PL>(g, ra, rb, i0, j0, sm, ubar, &tm, &tm2);
+    if (tile_interior<R>(a, g.s, ra, rb, i0, j0))
+        tma_tile_body<ST, R, VAR, PL, true>(a, lv, g, ra, rb, i0, j0, tid, ubar, sm);
     else
-        tma_tile_body<ST, R, VAR, PL, false>(a, lv, g, ra, rb, i0, j0, tid, ubar, sm, raw16);
+        tma_tile_body<ST, R, VAR, PL, false>(a, lv, g, ra, rb, i0, j0, tid, ubar, sm);
 }
 
 // ------------------------------------------------------------- REF-EXACT ----
