@@ -231,6 +231,26 @@ def algo_bytes_per_px(mode, storage):
     return 8 + 2 * 4 + 8
 
 
+def first_frames(steps, warmup, pool, event=30):
+    """(w0, t0): the sequence index of the first warm-up frame and of the first timed frame.
+
+    Steps walk the sequence in order (modulo its length).  When the timed steps cover less than the whole
+    sequence, the window is placed so that it holds `event` (the frame where a plane appears: a forced
+    disocclusion), and the warm-up frames are the ones just before it."""
+    if pool > event and steps < pool:
+        t0 = min(max(0, event - steps // 2), pool - steps)
+    else:
+        t0 = warmup % pool
+    return (t0 - warmup) % pool, t0
+
+
+def window_text(steps, t0, pool):
+    last = t0 + steps - 1
+    if steps >= pool:
+        return f"{steps} frames from sequence frame {t0}, cycling the {pool}-frame sequence (every frame, cuts included)"
+    return f"sequence frames {t0}..{last % pool}" + (" (wrapping: a camera cut)" if last >= pool else "")
+
+
 def run_tg(args, rank, world, local):
     import torch
 
@@ -249,8 +269,10 @@ def run_tg(args, rank, world, local):
     kpf = den.info()["kernels_per_frame"]
     stream = torch.cuda.current_stream()
 
+    w0, t0 = first_frames(args.steps, args.warmup, len(frames))
+
     def step(i):
-        fr = frames[i % len(frames)]
+        fr = frames[(w0 + i) % len(frames)]
         den.denoise(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=outs[i & 1])
 
     for i in range(args.warmup):
@@ -266,7 +288,7 @@ def run_tg(args, rank, world, local):
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     evs[0].record(stream)
     for i in range(args.steps):
-        step(args.warmup + i)
+        step(args.warmup + i)  # sequence frame (t0 + i) % pool
         evs[i + 1].record(stream)
     torch.cuda.synchronize()
     barrier(world)
@@ -287,13 +309,19 @@ def run_tg(args, rank, world, local):
            "config": {"workload": name, "width": W, "height": H, "mode": args.mode, "storage": args.storage,
                       "parallelism": f"replicas{world}" if world > 1 else "single",
                       "l2": "no flush: every frame's inputs (332 MB FP32) and state exceed the 126 MB L2",
-                      "frames_in_pool": args.pool},
+                      "frames_in_pool": args.pool, "timed_frames": window_text(args.steps, t0, len(frames)),
+                      "warmup_frames": f"the {args.warmup} sequence frames before the timed ones"},
            "mpx_per_s": value * px / 1e6,
            "p50_ms": per[len(per) // 2], "p99_ms": per[min(len(per) - 1, int(0.99 * len(per)))],
            "gpu_launches": kpf * args.steps}
     peak, peak_src = load_peaks()
     chain_bytes = algo_bytes_per_px(args.mode, args.storage) * px
-    res["chain_roofline"] = {"algo_bytes_per_px": algo_bytes_per_px(args.mode, args.storage),
+    # The path's roofline: the compulsory bytes of the whole chain per frame (inputs once, state read and written
+    # once, output once; a-trous scratch not counted) over the frame time.  `roofline` below is the dominant
+    # kernel's own figure.
+    res["chain_roofline"] = {"what": "the path's roofline: compulsory bytes of the whole chain per frame over the "
+                                     "frame time",
+                             "algo_bytes_per_px": algo_bytes_per_px(args.mode, args.storage),
                              "achieved": chain_bytes / (res["ms_per_step"] / 1e3) / 1e9, "peak": peak,
                              "unit": "GB/s", "peak_source": peak_src}
     res["chain_roofline"]["frac"] = res["chain_roofline"]["achieved"] / peak
@@ -322,7 +350,7 @@ def run_tg(args, rank, world, local):
     torch.cuda.synchronize()
 
     if not args.no_e2e:
-        res["e2e"] = run_e2e(args, frames, dev, mode, storage, world)
+        res["e2e"] = run_e2e(args, frames, dev, mode, storage, world, t0)
     else:
         res["e2e"] = None
     del frames
@@ -341,7 +369,7 @@ def run_tg(args, rank, world, local):
             res["accuracy"] = run_accuracy(dev)
         torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu:
-        res["cpu_baseline"] = run_cpu_baseline(args, spec, seconds=args.cpu_seconds)
+        res["cpu_baseline"] = run_cpu_baseline(args, spec, seconds=args.cpu_seconds, start=t0)
     return res
 
 
@@ -795,8 +823,20 @@ def run_serving(args, dev):
     return out
 
 
-def run_accuracy(dev, frames=33):
-    """Per-frame error of the FP32 and FP16 GPU paths against the float64 oracle (640x360, config-1 motion)."""
+def run_accuracy(dev, W=3840, H=2160, frames=60):
+    """The precision form's report: per-frame error of the FP32 and FP16-storage GPU paths against the float64
+    oracle over the whole 60-frame sequence at 3840x2160 (frames generated on the GPU, the oracle on every host
+    core).  Rows:
+      fp32          FP32 storage vs float64 on the same (full-precision) inputs;
+      fp16          FP16 storage (binary16 radiance, history, moments, octahedral normals) with an RGBA32F output
+                    image vs float64 on the same binary16 radiance and octahedral normals: the error of the
+                    FP16 state itself;
+      fp16_inputs   the same FP16 result vs float64 on the full-precision inputs: adds the rounding of the
+                    inputs to binary16 / octahedral codes;
+      fp16_out16    the FP16 result as an RGBA16F output image would hold it (the kernel rounds its float32
+                    output to nearest binary16 when it stores one) vs float64 on the same inputs.
+    Metrics on luminance: max |d|, max |d| / max(|ref|, 1e-3), relative L2, PSNR with the reference frame's
+    peak."""
     import numpy as np
     import torch
 
@@ -804,49 +844,69 @@ def run_accuracy(dev, frames=33):
     import tron_grid_gb300 as tg
     from tron_grid_gb300 import scene
 
-    W, H = 640, 360
-    sc = scene.PlaneScene(scene.config1(W, H, seed=0))
+    sc = scene.PlaneScene(scene.config1(W, H, seed=0), device=dev)
     d32 = tg.Denoiser(W, H, storage=tg.STORAGE_FP32, device=dev.index)
     d16 = tg.Denoiser(W, H, storage=tg.STORAGE_FP16, device=dev.index)
     st = oracle.FullState(H, W, np.float64)
+    stq = oracle.FullState(H, W, np.float64)
     P = oracle.full_params()
-    Y = np.array([0.2126, 0.7152, 0.0722])
-    rows = {"fp32": [], "fp16": []}
+    Y = torch.tensor([0.2126, 0.7152, 0.0722], dtype=torch.float64, device=dev)
+    o32 = torch.empty((H, W, 4), device=dev)
+    o16 = torch.empty((H, W, 4), device=dev)
+    names = ("fp32", "fp16", "fp16_inputs", "fp16_out16")
+    rows = {k: [] for k in names}
+    t_oracle = 0.0
+
+    def lum_of(ref):
+        return torch.from_numpy(ref[..., :3]).to(dev) @ Y
+
     for t in range(frames):
         fr = sc.frame(t)
-        ref, _ = oracle.full_frame(P, st, *(fr[k].numpy() for k in KEYS))
-        lr = ref[..., :3] @ Y
-        o32 = d32.denoise(*(fr[k].to(dev) for k in KEYS))
-        enc = oracle.oct16_encode(fr["normal"].numpy())
-        o16 = torch.empty((H, W, 4), dtype=torch.float16, device=dev)
-        d16.denoise(fr["radiance"].half().to(dev), fr["depth"].to(dev), torch.from_numpy(enc).to(dev),
-                    fr["motion"].to(dev), out=o16)
-        for name, o in (("fp32", o32), ("fp16", o16)):
-            lg = o.float().cpu().numpy()[..., :3] @ Y
-            d = lg - lr
-            mse = float(np.mean(d * d))
-            rows[name].append({"max_abs": float(np.abs(d).max()),
-                               "max_rel": float((np.abs(d) / np.maximum(np.abs(lr), 1e-3)).max()),
-                               "rel_l2": float(np.sqrt((d * d).sum() / (lr * lr).sum())),
-                               "psnr_db": float(10 * np.log10(lr.max() ** 2 / mse)) if mse > 0 else None})
+        rad16, enc = fr["radiance"].half(), scene.oct16_encode(fr["normal"])
+        d32.denoise(fr["radiance"], fr["depth"], fr["normal"], fr["motion"], out=o32)
+        d16.denoise(rad16, fr["depth"], enc, fr["motion"], out=o16)
+        dep, mot = fr["depth"].cpu().numpy(), fr["motion"].cpu().numpy()
+        c0 = time.perf_counter()
+        ref, _ = oracle.full_frame(P, st, fr["radiance"].cpu().numpy(), dep, fr["normal"].cpu().numpy(), mot)
+        refq, _ = oracle.full_frame(P, stq, rad16.float().cpu().numpy(), dep, oracle.oct16_decode(enc.cpu().numpy()),
+                                    mot)
+        t_oracle += time.perf_counter() - c0
+        lr, lq = lum_of(ref), lum_of(refq)
+        for name, o, l in (("fp32", o32, lr), ("fp16", o16, lq), ("fp16_inputs", o16, lr),
+                           ("fp16_out16", o16.half().float(), lq)):
+            d = o[..., :3].double() @ Y - l
+            mse = float((d * d).mean())
+            peak = float(l.abs().max())
+            rows[name].append({"max_abs": float(d.abs().max()),
+                               "max_rel": float((d.abs() / l.abs().clamp_min(1e-3)).max()),
+                               "rel_l2": float(torch.sqrt((d * d).sum() / (l * l).sum())),
+                               "psnr_db": 10 * float(np.log10(peak * peak / mse)) if mse > 0 else None})
     d32.close()
     d16.close()
-    out = {"workload": f"FULL {W}x{H}, {frames} frames (camera yaw + translation, plane at frame 30), vs float64 oracle"}
+    out = {"workload": f"FULL {W}x{H}, {frames} frames (camera yaw 0.5 deg + 0.05 m per frame, plane appears at "
+                       f"frame 30), GPU vs float64 oracle on {oracle.num_threads()} host threads "
+                       f"({t_oracle / frames:.2f} s per frame for the two float64 runs)",
+           "metric_floor": "relative errors divide by max(|reference luminance|, 1e-3)",
+           "bytes_per_px": {"fp32_algo": algo_bytes_per_px("full", "fp32"), "fp16_algo": algo_bytes_per_px("full", "fp16")}}
     for name, r in rows.items():
         ps = [x["psnr_db"] for x in r if x["psnr_db"] is not None]
-        out[name] = {"max_abs": max(x["max_abs"] for x in r), "max_rel": max(x["max_rel"] for x in r),
-                     "rel_l2_max": max(x["rel_l2"] for x in r), "psnr_db_min": min(ps) if ps else None}
+        worst = max(range(len(r)), key=lambda k: r[k]["max_rel"])
+        out[name] = {"max_abs": max(x["max_abs"] for x in r), "max_rel": r[worst]["max_rel"], "max_rel_frame": worst,
+                     "rel_l2_max": max(x["rel_l2"] for x in r), "psnr_db_min": min(ps) if ps else None,
+                     "per_frame": {k: [float(f"{x[k]:.4g}") if x[k] is not None else None for x in r]
+                                   for k in ("max_abs", "max_rel", "rel_l2", "psnr_db")}}
     return out
 
 
-def run_e2e(args, frames, dev, mode, storage, world):
-    """Frames/s through tg_svgf_denoise_host with pinned host buffers (copies in the timed region)."""
+def run_e2e(args, frames, dev, mode, storage, world, t0=0):
+    """Frames/s through tg_svgf_denoise_host with pinned host buffers (copies in the timed region); the host
+    frames are the sequence's frames from t0 on, cycled."""
     import torch
 
     import tron_grid_gb300 as tg
 
     n_host = min(8, len(frames))
-    host = [{k: v.cpu().pin_memory() for k, v in frames[i].items()} for i in range(n_host)]
+    host = [{k: v.cpu().pin_memory() for k, v in frames[(t0 + i) % len(frames)].items()} for i in range(n_host)]
     W, H = args.width, args.height
     out_dt = torch.float32 if args.storage == "fp32" else torch.float16
     houts = [torch.empty((H, W, 4), dtype=out_dt, pin_memory=True) for _ in range(3)]
@@ -864,23 +924,26 @@ def run_e2e(args, frames, dev, mode, storage, world):
     torch.cuda.synchronize()
     barrier(world)
     steps = args.steps
-    t0 = time.perf_counter()
+    c0 = time.perf_counter()
     for i in range(steps):
         step(i)
     den.synchronize()
     torch.cuda.synchronize()
-    t1 = time.perf_counter()
+    c1 = time.perf_counter()
     barrier(world)
-    el = max_over_ranks(t1 - t0, world, dev)
+    el = max_over_ranks(c1 - c0, world, dev)
     total = sum_over_ranks(float(steps), world, dev)
     den.close()
     return {"value": total / el, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": el / steps * 1e3, "host_frames_cycled": n_host,
+            "frames": f"sequence frames {t0}..{(t0 + n_host - 1) % len(frames)}, cycled",
             "api": "tg_svgf_denoise_host (pinned host buffers, a ring of three staging sets)"}
 
 
-def run_cpu_baseline(args, spec, seconds=15.0, frames=None):
-    """The float32 FULL oracle (a port of the path, OpenMP over rows) on the workload's own frames."""
+def run_cpu_baseline(args, spec, seconds=15.0, frames=None, start=0, warm=3):
+    """The float32 FULL oracle (a port of the path, OpenMP over rows, built for speed: oracle/build.py
+    TIMING_CXXFLAGS) on the workload's own sequence: `warm` untimed frames before sequence frame `start`, then
+    timed frames from `start` on, for `frames` frames or until `seconds` of CPU time."""
     import numpy as np
 
     import oracle
@@ -888,47 +951,55 @@ def run_cpu_baseline(args, spec, seconds=15.0, frames=None):
 
     sc = scene.PlaneScene(spec, device="cpu")
     W, H = spec.width, spec.height
+    pool = spec.frames
     if args.mode == "full":
         P = oracle.full_params()
         st = oracle.FullState(H, W, np.float32)
-    else:
-        mom = np.zeros((H, W, 2), np.float32)
-    done, el, t = 0, 0.0, 0
-    while True:
-        fr = sc.frame(t)
+    mom = np.zeros((H, W, 2), np.float32)
+    f16 = args.storage == "fp16"
+
+    def one(t):
+        nonlocal mom
+        fr = sc.frame(t % pool)
         arrs = [fr[k].numpy() for k in KEYS]
-        if args.storage == "fp16":
+        if f16:
             arrs[0] = arrs[0].astype(np.float16).astype(np.float32)
-        t0 = time.perf_counter()
+        c0 = time.perf_counter()
         if args.mode == "full":
-            oracle.full_frame(P, st, *arrs, fp16_store=args.storage == "fp16")
+            oracle.full_frame(P, st, *arrs, fp16_store=oracle.fp16_storage_mask(True) if f16 else 0, timing=True)
         else:
-            _, mom = oracle.ref_frame(arrs[0], mom, fp16_store=args.storage == "fp16")
-        el += time.perf_counter() - t0
+            _, mom = oracle.ref_frame(arrs[0], mom, fp16_store=f16, timing=True)
+        return time.perf_counter() - c0
+
+    for t in range(start - warm, start):
+        one(t)
+    done, el = 0, 0.0
+    while True:
+        el += one(start + done)
         done += 1
-        t += 1
         if (frames is not None and done >= frames) or (frames is None and el >= seconds):
             break
+    last = (start + done - 1) % pool
     return {"value": done / el, "unit": "frames/s", "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"frames 0..{done - 1} of the same {W}x{H} sequence ({el:.1f} s of CPU time, input "
-                      f"generation excluded)"}
+            "flags": oracle.timing_flags(),
+            "sample": f"sequence frames {start % pool}..{last} of the same {W}x{H} sequence after {warm} untimed "
+                      f"frames ({el:.1f} s of CPU time, input generation excluded)"}
 
 
 def run_reference(args, rank, world):
-    """CPU arm: the oracle port of the path on the host cores (the reference's shader cannot run here)."""
+    """CPU arm: the oracle port of the path on the host cores (the reference's shader cannot run here), over the
+    same warm-up and timed sequence frames as the GPU arm."""
     if rank != 0:
         return None
     spec, name = workload(args)
     import oracle
 
-    # Each step is one frame of the same sequence on all host threads (about a
-    # second at 4K); steps and warm-up frames are bounded so that the run ends
-    # within a few minutes.
-    steps = max(1, min(args.steps, 10))
-    warm = max(0, min(args.warmup, 3))
-    if warm:
-        run_cpu_baseline(args, spec, seconds=0.0, frames=warm)
-    base = run_cpu_baseline(args, spec, seconds=0.0, frames=steps)
+    # Each step is one frame on all host threads (about a second at 4K); steps and warm-up frames are those of
+    # the GPU arm up to 120 and 20, so that the run ends within a few minutes.
+    steps = max(1, min(args.steps, 120))
+    warm = max(0, min(args.warmup, 20))
+    w0, t0 = first_frames(steps, warm, spec.frames)
+    base = run_cpu_baseline(args, spec, seconds=0.0, frames=steps, start=t0, warm=warm)
     v = base["value"]
     res = {"metric": METRIC, "impl": "reference", "value": v, "unit": "frames/s", "n_gpus": world, "steps": steps,
            "warmup": warm, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",

@@ -50,3 +50,21 @@ def test_reference_arm_under_torchrun_prints_once():
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
     assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["n_gpus"] == 2
+
+
+def test_timed_window_holds_the_disocclusion():
+    """Whatever --steps and --warmup the driver passes, the timed frames of the 60-frame sequence hold frame 30
+    (where a plane appears) when they are fewer than the sequence, and the warm-up frames come just before them;
+    the reference arm times the same frames."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    for steps in (1, 2, 5, 20, 40, 59):
+        for warmup in (0, 3, 5, 20):
+            w0, t0 = bench.first_frames(steps, warmup, 60)
+            assert t0 <= 30 <= t0 + steps - 1 and t0 + steps <= 60, (steps, warmup, t0)
+            assert (w0 + warmup) % 60 == t0
+    assert bench.first_frames(20, 5, 60) == (15, 20)
+    w0, t0 = bench.first_frames(120, 5, 60)
+    assert t0 == 5 and w0 == 0
+    assert "20..39" in bench.window_text(20, 20, 60)
