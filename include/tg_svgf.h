@@ -373,14 +373,21 @@ TG_API void tg_svgf_server_destroy(tg_svgf_server* s);
  * packed, zero for the first frame) and denoised out.  The only scratch, the
  * two wavelet ping-pong images, lives in a fixed 16 MiB device array inside
  * this library, which every GPU that loads the library holds until exit.
- * That bounds the frame to about 1 Mpx with fp16 images (e.g. 1280x720) and
- * about 0.5 Mpx with fp32 images (e.g. 960x540); larger frames are rejected
- * with TG_ERR_INVALID.  params->mode must be TG_SVGF_MODE_REF_EXACT.
+ * With the default 3 levels that bounds the frame to about 1 Mpx with fp16
+ * images (e.g. 1280x720) and about 0.5 Mpx with fp32 images (e.g. 960x540);
+ * more levels pad the wavelet images further and lower the bound (at 10
+ * levels 960x540 fp32 no longer fits).  Frames that do not fit are rejected
+ * with TG_ERR_INVALID before anything is launched.  params->mode must be
+ * TG_SVGF_MODE_REF_EXACT.
  *
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  All calls share the array, so calls whose work overlaps on the GPU
- * race: serialise them (for example on one stream).  No call allocates. */
+ * Each CUDA context (one per device for runtime-API callers) has its own copy
+ * of the array.  The first call in a context looks up the array's device
+ * address in that context (the calling thread's current one) and caches it by
+ * the context's unique id; make that first call before any stream capture.
+ * Calls on different devices or in different contexts never share the array.
+ * Calls in the same context do, and the array keeps the last call's contents:
+ * calls whose work overlaps on the GPU race, so order them (one stream, or
+ * events between streams).  No call allocates. */
 #define TG_SVGF_NOALLOC_SCRATCH_BYTES (16u << 20)
 TG_API int tg_svgf_denoise_ref_noalloc(const tg_svgf_params* params, uint32_t width, uint32_t height,
                                        const tg_image* radiance, const tg_image* moments_prev,

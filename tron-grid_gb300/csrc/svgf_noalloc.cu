@@ -12,13 +12,16 @@
 // chain (src/svgf_denoise.slang:84-90), in the fixed device array below.
 //
 // The array lives in this library's device code: every GPU that loads the
-// library holds its 16 MiB until the process exits.  All calls share it, so
-// calls whose work overlaps on the GPU (different streams, or different host
-// threads) race on it; callers serialise them, e.g. on one stream.
+// library holds its 16 MiB until the process exits.  Each CUDA context on a
+// device has its own copy, so calls on different devices (or in different
+// contexts) never share it.  Calls in one context share it, so calls whose work
+// overlaps on the GPU (different streams, or different host threads) race on
+// it; callers order them, e.g. on one stream or with events.
 #include <cuda_runtime.h>
 
 #include <mutex>
 
+#include "noalloc_ctx_cache.h"
 #include "svgf_internal.h"
 #include "svgf_kernels.cuh"
 #include "svgf_level.cuh"
@@ -30,27 +33,59 @@ static_assert(kScratchBytes == TG_SVGF_NOALLOC_SCRATCH_BYTES, "header and librar
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
+// The array's device address belongs to a CUDA context, not to a device
+// number: a driver-API caller may run in a context other than the device's
+// primary one, and cudaDeviceReset replaces the primary context.  The address
+// is therefore cached per context (noalloc_ctx_cache.h), keyed by the
+// context's unique id, and looked up again for a context not seen before.
+// Without the driver entry points it is looked up on every call.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
 
-// Device address of the scratch on the current device, looked up once per
-// device (the host-side name of the array is not a device address).
+std::mutex g_setup_mu;
+tg::CtxAddrCache g_ctx_cache;
+
+void* driver_entry(const char* name)
+{
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+        p = nullptr;
+    cudaGetLastError();
+    return p;
+}
+
+// Unique id of the calling thread's current context (0 if it has none or it cannot be read).
+unsigned long long current_context_id()
+{
+    static CtxGetCurrentFn get_current = reinterpret_cast<CtxGetCurrentFn>(driver_entry("cuCtxGetCurrent"));
+    static CtxGetIdFn get_id = reinterpret_cast<CtxGetIdFn>(driver_entry("cuCtxGetId"));
+    if (!get_current || !get_id) return 0;
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of the scratch in the current context (the host-side name
+// of the array is not a device address).  The lookup makes the device's
+// primary context current on a thread that had none.
 int scratch_address(void** out)
 {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-        return tg::fail(TG_ERR_CUDA, "no usable current CUDA device");
+    if (cudaGetDevice(&dev) != cudaSuccess) return tg::fail(TG_ERR_CUDA, "no usable current CUDA device");
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return tg::fail(TG_ERR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch failed: %s",
-                            cudaGetErrorString(e));
-        g_scratch_ptr[dev] = p;
-    }
-    *out = g_scratch_ptr[dev];
+    cudaError_t err = cudaSuccess;
+    const int st = tg::ctx_cached_address(
+        g_ctx_cache, current_context_id,
+        [&err](void** p) {
+            err = cudaGetSymbolAddress(p, g_noalloc_scratch);
+            return (err == cudaSuccess && *p) ? 0 : 1;
+        },
+        out);
+    if (st)
+        return tg::fail(TG_ERR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch failed: %s", cudaGetErrorString(err));
     return TG_OK;
 }
 
