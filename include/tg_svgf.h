@@ -207,7 +207,7 @@ TG_API const char* tg_last_error(void);
  * the launch count, the summed event time and the summed compulsory bytes
  * (each buffer the kernel must read or write, counted once per pixel). */
 typedef struct tg_svgf_kernel_stat {
-    char name[32];     /* "ref_init", "ref_level", "full_temporal", "full_variance", "full_level" */
+    char name[32];     /* "ref_first", "ref_level", "full_temporal", "full_variance", "full_level" */
     uint32_t launches;
     uint32_t reserved;
     double total_ms;

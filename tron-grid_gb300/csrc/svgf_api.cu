@@ -210,8 +210,8 @@ template <bool PL> LevelTiledFn level_tiled_kernel(bool f16, bool last)
     if (f16) return last ? k_full_level_tiled<ST_FP16, kLevelR, false, PL> : k_full_level_tiled<ST_FP16, kLevelR, true, PL>;
     return last ? k_full_level_tiled<ST_FP32, kLevelR, false, PL> : k_full_level_tiled<ST_FP32, kLevelR, true, PL>;
 }
-enum Family { F_REF_INIT = 0, F_REF_LEVEL, F_FULL_TEMPORAL, F_FULL_VARIANCE, F_FULL_LEVEL, kFamilies };
-static const char* kFamilyName[kFamilies] = {"ref_init", "ref_level", "full_temporal", "full_variance", "full_level"};
+enum Family { F_REF_FIRST = 0, F_REF_LEVEL, F_FULL_TEMPORAL, F_FULL_VARIANCE, F_FULL_LEVEL, kFamilies };
+static const char* kFamilyName[kFamilies] = {"ref_first", "ref_level", "full_temporal", "full_variance", "full_level"};
 } // namespace tg
 
 struct tg_svgf {
@@ -512,37 +512,19 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         a.phi = s->p.sigma_l;
         a.alpha_m = s->p.moments_alpha;
         a.var_eps = s->p.variance_epsilon;
-        a.dst = s->colA;
         const double npx = double(s->w) * s->h;
         const double c4 = f16 ? 8 : 16, mm = f16 ? 4 : 8;
         const double rb = fmt_bytes(in->radiance.format), ob = fmt_bytes(out->denoised.format);
-        launch(s, stream, F_REF_INIT, npx * (rb + 2 * mm + c4), [&] {
-            if (f16)
-                k_ref_init<ST_FP16><<<grd, blk, 0, stream>>>(a);
-            else
-                k_ref_init<ST_FP32><<<grd, blk, 0, stream>>>(a);
+        const int levels = s->p.levels;
+        int lv = 0;
+        enqueue_ref_chain<kLevelR>(a, s->colA, s->colB, levels, f16, stream, [&](bool first, auto body) {
+            const bool last = lv == levels - 1;
+            // compulsory bytes: the fused pass reads radiance and moments_prev and writes moments_curr; every
+            // pass reads its input image and writes its output (the caller's image at the last pass)
+            const double bytes = npx * ((first ? rb + 2 * mm : c4) + (last ? ob : c4));
+            launch(s, stream, first ? F_REF_FIRST : F_REF_LEVEL, bytes, body);
+            ++lv;
         });
-        void* src = s->colA;
-        void* oth = s->colB;
-        for (int lv = 0; lv < s->p.levels; ++lv) {
-            a.src = src;
-            a.dst = oth;
-            a.stride = 1 << lv;
-            a.final_pass = lv == s->p.levels - 1;
-            a.lin = res_layout(a.w, a.h, lv);
-            a.lout = res_layout(a.w, a.h, lv + 1);
-            const LevelGeom lg = level_geom(a.w, a.h, a.stride, kLevelR);
-            const dim3 lgrid(level_blocks(lg)), lblk(kLvTX, kLvRows);
-            launch(s, stream, F_REF_LEVEL, npx * (c4 + (a.final_pass ? ob : c4)), [&] {
-                if (f16)
-                    k_ref_level_tiled<ST_FP16, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
-                else
-                    k_ref_level_tiled<ST_FP32, kLevelR><<<lgrid, lblk, 0, stream>>>(a, lg);
-            });
-            void* t = src;
-            src = oth;
-            oth = t;
-        }
     } else {
         FullArgs a{};
         a.w = int(s->w);

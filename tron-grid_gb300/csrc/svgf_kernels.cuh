@@ -39,7 +39,8 @@ __host__ __device__ inline ResLayout res_layout(int w, int h, int lg)
 }
 
 // ------------------------------------------------------------- REF-EXACT ----
-// src/svgf_denoise.slang:152-275, one kernel per pass.
+// src/svgf_denoise.slang:152-275: the arguments of the REF_EXACT kernels
+// (svgf_level.cuh; the init pass runs inside the first wavelet pass).
 
 struct RefArgs {
     int w, h;
@@ -56,31 +57,6 @@ struct RefArgs {
     int stride;
     int final_pass;
 };
-
-// Pass 0 (src/svgf_denoise.slang:176-191): luminance moments EMA, sqrt-variance.
-template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_ref_init(RefArgs a)
-{
-    typedef Stor<ST> S;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    if (x >= a.w || y >= a.h) return;
-    const size_t i = size_t(y) * a.w + x;
-    float4 c = ld_rgba(a.raw, x, y);
-    float l = lum(c.x, c.y, c.z);
-    float2 mp = S::ldm(static_cast<const typename S::mom_t*>(a.mom_prev), i);
-    float m1 = __fadd_rn(mp.x, __fmul_rn(__fsub_rn(l, mp.x), a.alpha_m));
-    float m2 = __fadd_rn(mp.y, __fmul_rn(__fsub_rn(__fmul_rn(l, l), mp.y), a.alpha_m));
-    float var = fmaxf(__fsub_rn(m2, __fmul_rn(m1, m1)), 0.0f);
-    float sd = __fsqrt_rn(__fadd_rn(var, a.var_eps));
-    typename S::mom_t* mc = static_cast<typename S::mom_t*>(a.mom_curr);
-    if (ST == ST_FP16) {
-        // rg16f store: plain round-to-nearest (overflows to inf as the reference does).
-        reinterpret_cast<uint32_t*>(mc)[i] = pack_h2(m1, m2);
-    } else {
-        S::stm(mc, i, make_float2(m1, m2));
-    }
-    S::st4(static_cast<typename S::c4_t*>(a.dst), i, make_float4(c.x, c.y, c.z, sd));
-}
 
 // ------------------------------------------------------------------ FULL ----
 

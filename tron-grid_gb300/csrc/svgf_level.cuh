@@ -582,78 +582,74 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
 }
 
 // ------------------------------------------------------------- REF-EXACT ----
-// src/svgf_denoise.slang:209-274 on the same tiling; staged coordinates are
-// clamped to the image (the reference's clamp-to-edge taps).
+// src/svgf_denoise.slang:176-274 on the same tiling; staged coordinates are
+// clamped to the image (the reference's clamp-to-edge taps).  The init pass
+// (src/svgf_denoise.slang:176-191) is pointwise, so it runs inside the first
+// a-trous pass: that kernel stages the caller's radiance as the init pass would
+// have stored it in wavelet_a (rounded to the storage format) and each centre
+// computes its own moments and sqrt-variance, so wavelet_a is never written
+// and read back.  Dispatches replaced: src/main.cpp:929-944 (one init and
+// three wavelet passes become three kernels).
 
-template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref_level_tiled(RefArgs a, LevelGeom g)
+// Whether the tile at (i0, j0) of residue (ra, rb), with its 2-cell halo, lies
+// inside a w x h image: then no staged coordinate needs clamping.
+template <int R> __device__ __forceinline__ bool ref_tile_interior(int w, int h, int s, int ra, int rb, int i0, int j0)
+{
+    typedef LevelTile<R> T;
+    return i0 >= 2 && j0 >= 2 && ra + s * (i0 + T::TX + 1) < w && rb + s * (j0 + T::TY + 1) < h;
+}
+
+// The 25 taps of this thread's R centres over the staged tile sA (r, g, b,
+// luminance) and the outputs.  ca: each centre's alpha (sqrt-variance as
+// stored), valid: the centre is a pixel of the image.  The colour and weight
+// sums accumulate in pairs (r, g) and (b, weight), one paired FMA each.
+template <int ST, int R>
+__device__ __forceinline__ void ref_taps_out(const RefArgs& a, int s, int ra, int rb, int i0, int j0, const float* ca,
+                                             const bool* valid, const float4* sA)
 {
     typedef Stor<ST> S;
     typedef typename S::c4_t C4;
     typedef LevelTile<R> T;
-    __shared__ float4 sA[T::N];
-
-    int ra, rb, i0, j0;
-    level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
-    const int s = g.s;
-    const C4* src = static_cast<const C4*>(a.src);
-    const int tid = threadIdx.y * kLvTX + threadIdx.x;
     const int ci = threadIdx.x, cj0 = threadIdx.y * R;
-    // each centre's alpha (the sigma of its luminance weight), loaded before the staging so that its latency
-    // overlaps it
-    float ca[R];
-    bool valid[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-        const int x = ra + s * (i0 + ci);
-        const int y = rb + s * (j0 + cj0 + k);
-        valid[k] = x < a.w && y < a.h;
-        ca[k] = valid[k] ? S::ld4_w(src, res_idx(a.lin, x, y)) : 0.f;
-    }
-    for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
-        const int si = k % T::SW, sj = k / T::SW;
-        const int x = min(max(ra + s * (i0 + si - 2), 0), a.w - 1);
-        const int y = min(max(rb + s * (j0 + sj - 2), 0), a.h - 1);
-        const float4 c = S::ld4(src, res_idx(a.lin, x, y));
-        sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
-    }
-    __syncthreads();
-
-    float lp[R], nk[R], ar[R], ag[R], ab[R], aw[R];
+    float lp[R], nk[R];
+    float2 rg[R], bw[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         lp[k] = sA[(cj0 + k + 2) * T::SW + ci + 2].w;
         const float sigma = fmaxf(__fmul_rn(a.phi, ca[k]), a.var_eps);
-        nk[k] = -kLog2e / sigma;
-        ar[k] = ag[k] = ab[k] = aw[k] = 0.f;
+        nk[k] = -kLog2e * rcp_approx(sigma);
+        rg[k] = bw[k] = make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int r = 0; r < R + 4; ++r) {
 #pragma unroll
         for (int dx = -2; dx <= 2; ++dx) {
             const float4 A = sA[(cj0 + r) * T::SW + ci + 2 + dx];
+            const float2 ag = make_float2(A.x, A.y), b1 = make_float2(A.z, 1.0f);
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const int dy = r - 2 - k;
                 if (dy < -2 || dy > 2) continue;
                 const float w = ex2_approx(fmaf(fabsf(A.w - lp[k]), nk[k], log2_b3(dx + 2) + log2_b3(dy + 2)));
-                ar[k] = fmaf(A.x, w, ar[k]);
-                ag[k] = fmaf(A.y, w, ag[k]);
-                ab[k] = fmaf(A.z, w, ab[k]);
-                aw[k] += w;
+                const float2 ww = make_float2(w, w);
+                rg[k] = fma2(ag, ww, rg[k]);
+                bw[k] = fma2(b1, ww, bw[k]);
             }
         }
     }
+    const int x = ra + s * (i0 + ci);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (!valid[k]) continue;
-        const int x = ra + s * (i0 + ci);
         const int y = rb + s * (j0 + cj0 + k);
-        const int c = (cj0 + k + 2) * T::SW + ci + 2;
         float4 o;
-        if (aw[k] > 1e-6f)
-            o = make_float4(__fdiv_rn(ar[k], aw[k]), __fdiv_rn(ag[k], aw[k]), __fdiv_rn(ab[k], aw[k]), ca[k]);
-        else
-            o = make_float4(sA[c].x, sA[c].y, sA[c].z, ca[k]);
+        if (bw[k].y > 1e-6f) {
+            const float inv = rcp_approx(bw[k].y);
+            o = make_float4(rg[k].x * inv, rg[k].y * inv, bw[k].x * inv, ca[k]);
+        } else {
+            const float4 c = sA[(cj0 + k + 2) * T::SW + ci + 2];
+            o = make_float4(c.x, c.y, c.z, ca[k]);
+        }
         if (a.final_pass) {
             if (ST == ST_FP16) o = make_float4(q16(o.x), q16(o.y), q16(o.z), 1.0f);
             o.w = 1.0f;
@@ -662,6 +658,129 @@ template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref
             S::st4(static_cast<C4*>(a.dst), res_idx(a.lout, x, y), o);
         }
     }
+}
+
+// Init and the first wavelet pass (stride 1) in one kernel: reads the caller's
+// radiance and moments_prev, writes moments_curr and the pass's output (the
+// next pass's input, or the caller's image when it is the only pass).
+template <int ST, int R, bool IN>
+__device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0, float4* sA)
+{
+    typedef Stor<ST> S;
+    typedef typename S::mom_t M;
+    typedef LevelTile<R> T;
+    const int tid = threadIdx.y * kLvTX + threadIdx.x;
+    const int ci = threadIdx.x, cj0 = threadIdx.y * R;
+    float ca[R];
+    bool valid[R];
+    float4 craw[R];
+    float2 mp[R];
+    // each centre's radiance and previous moments, loaded before the staging so that their latency overlaps it
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int x = i0 + ci, y = j0 + cj0 + k;
+        valid[k] = IN || (x < a.w && y < a.h);
+        craw[k] = valid[k] ? ld_rgba(a.raw, x, y) : make_float4(0.f, 0.f, 0.f, 0.f);
+        mp[k] = valid[k] ? S::ldm(static_cast<const M*>(a.mom_prev), size_t(y) * a.w + x) : make_float2(0.f, 0.f);
+    }
+    for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+        const int sj = k / T::SW, si = k - sj * T::SW;
+        int x = i0 + si - 2, y = j0 + sj - 2;
+        if (!IN) {
+            x = min(max(x, 0), a.w - 1);
+            y = min(max(y, 0), a.h - 1);
+        }
+        // wavelet_a's colour as the init pass stores it: the radiance in the storage format
+        const float4 c = S::rt4(ld_rgba(a.raw, x, y));
+        sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
+    }
+    // src/svgf_denoise.slang:177-190: moments EMA and sqrt-variance (the alpha wavelet_a would carry)
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const float l = lum(craw[k].x, craw[k].y, craw[k].z);
+        const float m1 = __fadd_rn(mp[k].x, __fmul_rn(__fsub_rn(l, mp[k].x), a.alpha_m));
+        const float m2 = __fadd_rn(mp[k].y, __fmul_rn(__fsub_rn(__fmul_rn(l, l), mp[k].y), a.alpha_m));
+        const float var = fmaxf(__fsub_rn(m2, __fmul_rn(m1, m1)), 0.0f);
+        const float sd = __fsqrt_rn(__fadd_rn(var, a.var_eps));
+        ca[k] = ST == ST_FP16 ? q16(sd) : sd;
+        if (valid[k]) {
+            const size_t i = size_t(j0 + cj0 + k) * a.w + (i0 + ci);
+            if (ST == ST_FP16)
+                // rg16f store: plain round-to-nearest (overflows to inf as the reference's image store does)
+                reinterpret_cast<uint32_t*>(a.mom_curr)[i] = pack_h2(m1, m2);
+            else
+                S::stm(static_cast<M*>(a.mom_curr), i, make_float2(m1, m2));
+        }
+    }
+    __syncthreads();
+    ref_taps_out<ST, R>(a, 1, 0, 0, i0, j0, ca, valid, sA);
+}
+
+template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref_first(RefArgs a, LevelGeom g)
+{
+    typedef LevelTile<R> T;
+    __shared__ float4 sA[T::N];
+    const int i0 = int(blockIdx.x % unsigned(g.tiles_x)) * T::TX;
+    const int j0 = int(blockIdx.x / unsigned(g.tiles_x)) * T::TY;
+    if (ref_tile_interior<R>(a.w, a.h, 1, 0, 0, i0, j0))
+        ref_first_tile<ST, R, true>(a, i0, j0, sA);
+    else
+        ref_first_tile<ST, R, false>(a, i0, j0, sA);
+}
+
+// One wavelet pass at stride s >= 2 over residue-major scratch.
+template <int ST, int R, bool IN>
+__device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, int rb, int i0, int j0, float4* sA)
+{
+    typedef Stor<ST> S;
+    typedef typename S::c4_t C4;
+    typedef LevelTile<R> T;
+    const C4* src = static_cast<const C4*>(a.src);
+    const int tid = threadIdx.y * kLvTX + threadIdx.x;
+    const int ci = threadIdx.x, cj0 = threadIdx.y * R;
+    const int pw = a.lin.pw;
+    // each centre's alpha (the sigma of its luminance weight), loaded before the staging so that its latency
+    // overlaps it
+    float ca[R];
+    bool valid[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int x = ra + s * (i0 + ci);
+        const int y = rb + s * (j0 + cj0 + k);
+        valid[k] = IN || (x < a.w && y < a.h);
+        ca[k] = valid[k] ? S::ld4_w(src, res_idx(a.lin, x, y)) : 0.f;
+    }
+    if (IN) {
+        // the tile's plane rows are contiguous runs of the residue-major layout
+        const int base = ((rb << a.lin.lg) + ra) * a.lin.ph * pw + (j0 - 2) * pw + (i0 - 2);
+        for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+            const int sj = k / T::SW, si = k - sj * T::SW;
+            const float4 c = S::ld4(src, base + sj * pw + si);
+            sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
+        }
+    } else {
+        for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+            const int sj = k / T::SW, si = k - sj * T::SW;
+            const int x = min(max(ra + s * (i0 + si - 2), 0), a.w - 1);
+            const int y = min(max(rb + s * (j0 + sj - 2), 0), a.h - 1);
+            const float4 c = S::ld4(src, res_idx(a.lin, x, y));
+            sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
+        }
+    }
+    __syncthreads();
+    ref_taps_out<ST, R>(a, s, ra, rb, i0, j0, ca, valid, sA);
+}
+
+template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref_level(RefArgs a, LevelGeom g)
+{
+    typedef LevelTile<R> T;
+    __shared__ float4 sA[T::N];
+    int ra, rb, i0, j0;
+    level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
+    if (ref_tile_interior<R>(a.w, a.h, g.s, ra, rb, i0, j0))
+        ref_level_tile<ST, R, true>(a, g.s, ra, rb, i0, j0, sA);
+    else
+        ref_level_tile<ST, R, false>(a, g.s, ra, rb, i0, j0, sA);
 }
 
 __host__ __device__ inline LevelGeom level_geom(int w, int h, int s, int R)
@@ -680,6 +799,50 @@ __host__ __device__ inline LevelGeom level_geom(int w, int h, int s, int R)
 __host__ __device__ inline unsigned level_blocks(const LevelGeom& g)
 {
     return unsigned(g.s * g.s) * g.tiles_x * g.tiles_y;
+}
+
+// Enqueues one REF_EXACT frame on `stream`: the init fused into the first pass
+// (stride 1, output to `wb`), then passes at strides 2, 4, ... alternating
+// wb -> wa -> wb; the last pass writes the caller's image.  `a` carries the
+// images and constants.  hook(first, body) runs each launch body (first: the
+// fused pass), so that a caller can bracket it with events.
+template <int R, class Hook>
+void enqueue_ref_chain(RefArgs a, void* wa, void* wb, int levels, bool f16, cudaStream_t stream, Hook hook)
+{
+    const dim3 blk(kLvTX, kLvRows);
+    a.src = nullptr;
+    a.dst = wb;
+    a.stride = 1;
+    a.final_pass = levels == 1;
+    a.lin = res_layout(a.w, a.h, 0);
+    a.lout = res_layout(a.w, a.h, 1);
+    const LevelGeom g0 = level_geom(a.w, a.h, 1, R);
+    hook(true, [&] {
+        if (f16)
+            k_ref_first<ST_FP16, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0);
+        else
+            k_ref_first<ST_FP32, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0);
+    });
+    void* src = wb;
+    void* oth = wa;
+    for (int lv = 1; lv < levels; ++lv) {
+        a.src = src;
+        a.dst = oth;
+        a.stride = 1 << lv;
+        a.final_pass = lv == levels - 1;
+        a.lin = res_layout(a.w, a.h, lv);
+        a.lout = res_layout(a.w, a.h, lv + 1);
+        const LevelGeom g = level_geom(a.w, a.h, a.stride, R);
+        hook(false, [&] {
+            if (f16)
+                k_ref_level<ST_FP16, R><<<level_blocks(g), blk, 0, stream>>>(a, g);
+            else
+                k_ref_level<ST_FP32, R><<<level_blocks(g), blk, 0, stream>>>(a, g);
+        });
+        void* t = src;
+        src = oth;
+        oth = t;
+    }
 }
 
 } // namespace tg

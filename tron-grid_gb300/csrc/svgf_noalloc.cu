@@ -89,11 +89,13 @@ int scratch_address(void** out)
     return TG_OK;
 }
 
-// Pixels of one wavelet image in the residue-major layouts of strides 1 .. 2^(levels-1).
+// Pixels of one wavelet image in the residue-major layouts of strides
+// 2 .. 2^(levels-1), the layouts the passes hand on (the first pass reads the
+// caller's radiance and the last writes the caller's image).
 size_t wavelet_pixels(int levels, uint32_t w, uint32_t h)
 {
     size_t n = 0;
-    for (int lg = 0; lg < levels; ++lg) {
+    for (int lg = 1; lg < levels; ++lg) {
         const size_t s = size_t(1) << lg;
         const size_t m = s * s * ((w + s - 1) / s) * ((h + s - 1) / s);
         n = m > n ? m : n;
@@ -138,9 +140,9 @@ extern "C" int tg_svgf_denoise_ref_noalloc(const tg_svgf_params* params, uint32_
 
     void* scratch = nullptr;
     if ((st = scratch_address(&scratch))) return st;
-    // Nothing in the scratch has to start at zero: the init pass writes every
-    // pixel of wavelet image A before a level reads it, each level writes every
-    // pixel it hands to the next, and layout padding is never read.
+    // Nothing in the scratch has to start at zero: each pass writes every pixel
+    // it hands to the next (the first pass reads only the caller's images), and
+    // layout padding is never read.
     char* wa = static_cast<char*>(scratch);
     char* wb = wa + img_bytes;
 
@@ -159,33 +161,7 @@ extern "C" int tg_svgf_denoise_ref_noalloc(const tg_svgf_params* params, uint32_
     a.phi = params->sigma_l;
     a.alpha_m = params->moments_alpha;
     a.var_eps = params->variance_epsilon;
-    a.dst = wa;
-    const dim3 blk(kBlockX, kBlockY);
-    const dim3 grd((width + kBlockX - 1) / kBlockX, (height + kBlockY - 1) / kBlockY);
-    if (f16)
-        k_ref_init<ST_FP16><<<grd, blk, 0, stream>>>(a);
-    else
-        k_ref_init<ST_FP32><<<grd, blk, 0, stream>>>(a);
-    void* src = wa;
-    void* oth = wb;
-    constexpr int R = 2;
-    for (int lv = 0; lv < params->levels; ++lv) {
-        a.src = src;
-        a.dst = oth;
-        a.stride = 1 << lv;
-        a.final_pass = lv == params->levels - 1;
-        a.lin = res_layout(a.w, a.h, lv);
-        a.lout = res_layout(a.w, a.h, lv + 1);
-        const LevelGeom g = level_geom(a.w, a.h, a.stride, R);
-        const dim3 lgrid(level_blocks(g)), lblk(kLvTX, kLvRows);
-        if (f16)
-            k_ref_level_tiled<ST_FP16, R><<<lgrid, lblk, 0, stream>>>(a, g);
-        else
-            k_ref_level_tiled<ST_FP32, R><<<lgrid, lblk, 0, stream>>>(a, g);
-        void* t = src;
-        src = oth;
-        oth = t;
-    }
+    enqueue_ref_chain<2>(a, wa, wb, params->levels, f16, stream, [](bool, auto body) { body(); });
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TG_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
     return TG_OK;
