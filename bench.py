@@ -59,9 +59,9 @@ def parse_args(argv=None):
     ap.add_argument("--serve-sessions", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-rate", type=float, default=4000.0)
-    ap.add_argument("--only", choices=("fog", "post", "eye"), default=None,
-                    help="run one widening line alone (froxel filter, bloom + post-process, eye readback) for --steps "
-                         "timed frames and print its JSON; one GPU")
+    ap.add_argument("--only", choices=("fog", "post", "eye", "batched", "serving"), default=None,
+                    help="run one line alone (froxel filter, bloom + post-process, eye readback for --steps timed "
+                         "frames; the batched or the serving form) and print its JSON; one GPU")
     return ap.parse_args(argv)
 
 
@@ -786,6 +786,13 @@ def run_serving(args, dev):
         for tk in list(pending.values()):
             lat.append(server.wait(tk))
         st = server.stats()
+        ok = [x for x in lat if x["status"] == 0]
+        q = np.sort([x["queue_ms"] for x in ok]) if ok else np.zeros(1)
+        sv_ms = np.sort([x["latency_ms"] - x["queue_ms"] for x in ok]) if ok else np.zeros(1)
+        st["queue_p50_ms"], st["queue_p99_ms"] = float(q[len(q) // 2]), float(q[min(len(q) - 1, int(0.99 * len(q)))])
+        st["service_p50_ms"] = float(sv_ms[len(sv_ms) // 2])
+        st["service_p99_ms"] = float(sv_ms[min(len(sv_ms) - 1, int(0.99 * len(sv_ms)))])
+        st["mean_batch"] = float(np.mean([x["batch_size"] for x in ok])) if ok else 0.0
         return st
 
     out = {"workload": f"{n} sessions from {res_set} (weights {weights}), Poisson {args.serve_rate:.0f} frames/s for "
@@ -815,7 +822,10 @@ def run_serving(args, dev):
             res[mode] = {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
                          "mpx_per_s": st["mpx_per_s"], "completed": st["completed"], "failed": st["failed"],
                          "launches": st["launches"], "max_batch": st["max_batch_seen"],
-                         "evictions": st["evictions"], "peak_resident_gb": st["peak_resident_bytes"] / 2 ** 30}
+                         "evictions": st["evictions"], "peak_resident_gb": st["peak_resident_bytes"] / 2 ** 30,
+                         "queue_p50_ms": st["queue_p50_ms"], "queue_p99_ms": st["queue_p99_ms"],
+                         "service_p50_ms": st["service_p50_ms"], "service_p99_ms": st["service_p99_ms"],
+                         "mean_batch_of_a_request": st["mean_batch"]}
             sv.stats(reset=True)
         sv.close()
         out[name] = res
@@ -1038,6 +1048,10 @@ def main(argv=None):
 
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
+        if args.only in ("batched", "serving"):
+            fn = run_batched if args.only == "batched" else run_serving
+            print(json.dumps({args.only: fn(args, dev)}), flush=True)
+            return
         fn = {"fog": run_fog, "post": run_post, "eye": run_eye}[args.only]
         print(json.dumps({args.only: fn(args, dev, steps=args.steps, cpu=not args.no_cpu)}), flush=True)
         return

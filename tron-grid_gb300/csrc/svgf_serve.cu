@@ -3,9 +3,12 @@
 //
 // Threads.  Producers call tg_svgf_server_submit from any thread; a scheduler
 // thread forms launches; a completion thread waits for each launch's result
-// copy and completes its tickets.  At most two launches are in flight: while
-// launch k computes, the inputs of launch k+1 are already being copied in (on
-// a separate copy stream), and the outputs of k-1 copied out.
+// copy and completes its tickets.  Up to kMaxInflight launches are in flight:
+// while launch k computes, the inputs of the launches after it are already
+// being copied in (on a separate copy stream), and the outputs of k-1 copied
+// out.  A session has at most two frames in flight, because its staging slots
+// alternate by frame parity.  Completion events come from a pool and are
+// reused.
 //
 // Memory.  One device allocation of the budget holds every resident session;
 // a first-fit allocator hands out one block per session: state (guide,
@@ -124,10 +127,18 @@ struct Sess {
     char* out_slot[2];
     uint64_t frames = 0, lru = 0;
     int pending = 0;  // queued + running frames
+    int running = 0;  // frames in launches not yet complete (at most 2)
 };
+
+// Launches in flight at once (each with its own work table and graph).
+#ifndef TG_SERVE_MAX_INFLIGHT
+#define TG_SERVE_MAX_INFLIGHT 3
+#endif
+constexpr int kMaxInflight = TG_SERVE_MAX_INFLIGHT;
 
 struct Flight {
     std::vector<Req*> reqs;
+    std::vector<Sess*> sess;
     cudaEvent_t ev_comp = nullptr, ev_d2h = nullptr;
     int table_k = -1;
 };
@@ -154,11 +165,12 @@ struct tg_svgf_server {
     // persistent-launch machinery (batching)
     int cap = 0, grid = 0, launches = 0;
     size_t tbytes = 0;
-    char* d_table[2] = {nullptr, nullptr};
-    char* h_table[2] = {nullptr, nullptr};
+    char* d_table[kMaxInflight] = {};
+    char* h_table[kMaxInflight] = {};
     int* h_err = nullptr;
     BarrierState* d_bar = nullptr;
-    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaGraphExec_t exec[kMaxInflight] = {};
+    std::vector<cudaEvent_t> ev_pool;  // completion events, reused
     bool graphs_ok = true;
     // stats
     uint64_t submitted = 0, completed = 0, failed = 0, admissions = 0, evictions = 0, n_launches = 0;
@@ -173,7 +185,6 @@ struct tg_svgf_server {
 namespace {
 
 constexpr int kR = 2;
-constexpr int kMaxInflight = 2;
 
 using StepFn = void (*)(const char*, int, BarrierState*, unsigned, long long);
 StepFn step_kernel(bool f16) { return f16 ? k_batch_step<ST_FP16, kR> : k_batch_step<ST_FP32, kR>; }
@@ -446,6 +457,20 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
     }
 }
 
+// A completion event from the pool (created when the pool is empty); the
+// caller holds sv->mu.
+cudaEvent_t pool_event(tg_svgf_server* sv)
+{
+    if (!sv->ev_pool.empty()) {
+        cudaEvent_t e = sv->ev_pool.back();
+        sv->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    return e;
+}
+
 void finish(tg_svgf_server* sv, Req* r, int status, Clock::time_point now)
 {
     r->status = status;
@@ -494,7 +519,7 @@ void scheduler(tg_svgf_server* sv)
                     }
                     continue;
                 }
-                if (std::find(busy.begin(), busy.end(), s.id) != busy.end()) {
+                if (s.running >= 2 || std::find(busy.begin(), busy.end(), s.id) != busy.end()) {
                     ++it;
                     continue;
                 }
@@ -531,6 +556,7 @@ void scheduler(tg_svgf_server* sv)
                 if (s.fresh) fresh.push_back(&s);
                 s.fresh = false;
                 busy.push_back(s.id);
+                s.running++;
                 batch_px += uint64_t(r->w) * r->h;
                 batch.push_back(r);
                 ss.push_back(&s);
@@ -548,7 +574,7 @@ void scheduler(tg_svgf_server* sv)
             }
         }
         if (failed_any) sv->cv_done.notify_all();
-        const int k = batch_no & 1;
+        const int k = batch_no % kMaxInflight;
         // inputs in (copy stream); slots alternate by frame parity
         for (size_t j = 0; j < batch.size(); ++j) {
             Req* r = batch[j];
@@ -567,9 +593,13 @@ void scheduler(tg_svgf_server* sv)
         for (Sess* s : fresh) cudaMemsetAsync(s->state, 0, s->state_len, sv->s_comp);
         Flight* fl = new Flight();
         fl->reqs = batch;
+        fl->sess = ss;
         fl->table_k = (sv->d.batching && sv->d.strategy == TG_SVGF_BATCH_PERSISTENT) ? k : -1;
-        cudaEventCreateWithFlags(&fl->ev_comp, cudaEventDisableTiming);
-        cudaEventCreateWithFlags(&fl->ev_d2h, cudaEventDisableTiming);
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            fl->ev_comp = pool_event(sv);
+            fl->ev_d2h = pool_event(sv);
+        }
         const Clock::time_point tl = Clock::now();
         if (sv->d.batching)
             launch_batch(sv, ss, k);
@@ -626,6 +656,7 @@ void completer(tg_svgf_server* sv)
         const Clock::time_point now = Clock::now();
         {
             std::lock_guard<std::mutex> lk(sv->mu);
+            for (Sess* s : fl->sess) s->running--;
             for (Req* r : fl->reqs) {
                 finish(sv, r, status, now);
                 Sess& s = sv->sess[r->session];
@@ -637,9 +668,9 @@ void completer(tg_svgf_server* sv)
                 }
             }
             sv->inflight.pop_front();
+            sv->ev_pool.push_back(fl->ev_comp);
+            sv->ev_pool.push_back(fl->ev_d2h);
         }
-        cudaEventDestroy(fl->ev_comp);
-        cudaEventDestroy(fl->ev_d2h);
         delete fl;
         sv->cv_done.notify_all();
         sv->cv_work.notify_all();
@@ -650,10 +681,11 @@ void teardown(tg_svgf_server* sv)
 {
     for (auto& e : sv->exec)
         if (e) cudaGraphExecDestroy(e);
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < kMaxInflight; ++k) {
         if (sv->d_table[k]) cudaFree(sv->d_table[k]);
         if (sv->h_table[k]) cudaFreeHost(sv->h_table[k]);
     }
+    for (cudaEvent_t e : sv->ev_pool) cudaEventDestroy(e);
     if (sv->h_err) cudaFreeHost(sv->h_err);
     if (sv->d_bar) cudaFree(sv->d_bar);
     if (sv->base) cudaFree(sv->base);
@@ -720,16 +752,16 @@ int tg_svgf_server_create(const tg_svgf_server_desc* d, tg_svgf_server** out)
         sv->grid = nb * sv->sm_count;
         sv->cap = int(d->max_batch);
         sv->tbytes = table_bytes(sv->cap);
-        for (int k = 0; k < 2; ++k)
+        for (int k = 0; k < kMaxInflight; ++k)
             if (cudaMalloc(&sv->d_table[k], sv->tbytes) != cudaSuccess ||
                 cudaHostAlloc(reinterpret_cast<void**>(&sv->h_table[k]), sv->tbytes, cudaHostAllocDefault) !=
                     cudaSuccess)
                 return bail(fail(TG_ERR_OOM, "work table allocation failed"));
-        if (cudaHostAlloc(reinterpret_cast<void**>(&sv->h_err), 2 * sizeof(int), cudaHostAllocDefault) !=
+        if (cudaHostAlloc(reinterpret_cast<void**>(&sv->h_err), kMaxInflight * sizeof(int), cudaHostAllocDefault) !=
                 cudaSuccess ||
             cudaMalloc(&sv->d_bar, sizeof(BarrierState)) != cudaSuccess)
             return bail(fail(TG_ERR_OOM, "barrier allocation failed"));
-        sv->h_err[0] = sv->h_err[1] = 0;
+        for (int k = 0; k < kMaxInflight; ++k) sv->h_err[k] = 0;
     }
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(TG_ERR_CUDA, "server initialisation failed"));
     try {
