@@ -62,19 +62,6 @@ __device__ __forceinline__ float sqrt_approx(float x)
     return y;
 }
 
-// Lane-wise a * b + c on a pair of floats in one instruction (the paired FP32
-// form sm_100-class GPUs issue: fma.rn.f32x2, each half rounded as fmaf).
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
-{
-    float2 d;
-    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
-        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
-        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(d.x), "=f"(d.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return d;
-}
-
 __device__ __forceinline__ float b3(int i)
 {
     // B3-spline taps 1/16, 1/4, 3/8, 1/4, 1/16 (index 0..4).

@@ -601,8 +601,9 @@ template <int R> __device__ __forceinline__ bool ref_tile_interior(int w, int h,
 
 // The 25 taps of this thread's R centres over the staged tile sA (r, g, b,
 // luminance) and the outputs.  ca: each centre's alpha (sqrt-variance as
-// stored), valid: the centre is a pixel of the image.  The colour and weight
-// sums accumulate in pairs (r, g) and (b, weight), one paired FMA each.
+// stored), valid: the centre is a pixel of the image.  (Accumulating the sums
+// in paired FMAs, fma.rn.f32x2, was measured 1% slower: the broadcast of each
+// weight to both halves costs a move.)
 template <int ST, int R>
 __device__ __forceinline__ void ref_taps_out(const RefArgs& a, int s, int ra, int rb, int i0, int j0, const float* ca,
                                              const bool* valid, const float4* sA)
@@ -625,15 +626,15 @@ __device__ __forceinline__ void ref_taps_out(const RefArgs& a, int s, int ra, in
 #pragma unroll
         for (int dx = -2; dx <= 2; ++dx) {
             const float4 A = sA[(cj0 + r) * T::SW + ci + 2 + dx];
-            const float2 ag = make_float2(A.x, A.y), b1 = make_float2(A.z, 1.0f);
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const int dy = r - 2 - k;
                 if (dy < -2 || dy > 2) continue;
                 const float w = ex2_approx(fmaf(fabsf(A.w - lp[k]), nk[k], log2_b3(dx + 2) + log2_b3(dy + 2)));
-                const float2 ww = make_float2(w, w);
-                rg[k] = fma2(ag, ww, rg[k]);
-                bw[k] = fma2(b1, ww, bw[k]);
+                rg[k].x = fmaf(A.x, w, rg[k].x);
+                rg[k].y = fmaf(A.y, w, rg[k].y);
+                bw[k].x = fmaf(A.z, w, bw[k].x);
+                bw[k].y += w;
             }
         }
     }
