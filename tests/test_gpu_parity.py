@@ -293,3 +293,31 @@ def test_tma_and_plain_staging_agree(cuda_dev, storage, W):
         assert torch.equal(oa, ob), f"frame {t}"
     a.synchronize()
     assert a.info()["device_errors"] == 0
+
+
+@pytest.mark.parametrize("storage", [tg.STORAGE_FP32, tg.STORAGE_FP16])
+@pytest.mark.parametrize("W,H,pitch_px", [(333, 197, 0), (334, 197, 0), (640, 360, 0), (640, 360, 648)])
+def test_ref_exact_tma_and_plain_staging_agree(cuda_dev, storage, W, H, pitch_px):
+    """REF_EXACT: interior tiles staged by the tensor-memory accelerator (the first pass from the caller's
+    radiance, the later ones from the residue planes) give the same bits as plain loads, for radiance images
+    that are tightly packed or pitched, in either storage format; a width whose plane rows are not a multiple
+    of 16 bytes falls back to plain loads for that pass."""
+    f16 = storage == tg.STORAGE_FP16
+    dt = torch.float16 if f16 else torch.float32
+    a = tg.Denoiser(W, H, mode=tg.MODE_REF_EXACT, storage=storage)
+    b = tg.Denoiser(W, H, mode=tg.MODE_REF_EXACT, storage=storage, flags=tg._lib.FLAG_NO_TMA)
+    assert a.info()["tma"] == 1 and b.info()["tma"] == 0
+    sc = scene.PlaneScene(scene.config1(W, H, seed=13), device=cuda_dev)
+    for t in range(4):
+        rad = sc.frame(t)["radiance"].to(dt)
+        if pitch_px:
+            big = torch.zeros((H, pitch_px, 4), dtype=dt, device=cuda_dev)
+            big[:, :W] = rad
+            rad = big[:, :W]
+        oa = a.denoise(rad, out=torch.empty((H, W, 4), dtype=dt, device=cuda_dev))
+        ob = b.denoise(rad, out=torch.empty((H, W, 4), dtype=dt, device=cuda_dev))
+        assert torch.equal(oa, ob), f"frame {t}"
+    a.synchronize()
+    assert a.info()["device_errors"] == 0
+    a.close()
+    b.close()

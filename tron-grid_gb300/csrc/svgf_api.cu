@@ -162,7 +162,7 @@ size_t scratch_bytes_of(const tg_svgf_params& p, uint32_t w, uint32_t h)
     const size_t n = size_t(w) * h;
     const Layout l = layout_of(p);
     const size_t col = col_bytes_of(p, w, h);
-    if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * col;
+    if (p.mode == TG_SVGF_MODE_REF_EXACT) return 2 * col + 256;  // + the device error word
     return align_up(n * l.c4, 256) + 2 * col + align_up(n * sizeof(float) * 2, 256) + align_up(fb_flags_bytes_of(w, h), 256) +
            256;
 }
@@ -238,6 +238,15 @@ struct tg_svgf {
     CUtensorMap tmaps[10];           // per level: the level's input records
     bool tma0 = false;               // level 0 staged by TMA from the tc and guide planes
     CUtensorMap tm_tc, tm_guide[2];  // row-major tc and guide[parity] (level 0 reads these, not records)
+    // REF_EXACT: maps over each later pass's input planes, and over the caller's radiance (re-encoded when the
+    // caller's buffer, pitch or format changes)
+    bool ref_lv_ok[10] = {};
+    CUtensorMap ref_lv[10];
+    bool ref_in_ok = false;
+    const void* ref_in_ptr = nullptr;
+    int64_t ref_in_pitch = 0;
+    int32_t ref_in_fmt = -1;
+    CUtensorMap ref_in;
     // host-call staging: a ring of three sets, so that a frame's upload never
     // waits for the download of the frame two before it
     static constexpr int kStaging = 3;
@@ -300,7 +309,7 @@ void carve(tg_svgf* s)
         s->guide[0] = s->guide[1] = s->hist[0] = s->hist[1] = s->tc = nullptr;
         s->grad = nullptr;
         s->fb_flags = nullptr;
-        s->d_err = nullptr;
+        s->d_err = static_cast<int*>(take(sizeof(int)));
     } else {
         for (int k = 0; k < 2; ++k) {
             s->guide[k] = take(n * l.guide);
@@ -341,12 +350,74 @@ EncodeTiledFn encode_tiled()
 // the residue-major layout of stride 2^L: {float, row, plane, half-plane};
 // box = one 36 x 20 halo tile, whose rows are contiguous lines.
 // Level 0 has no records: its maps cover the tc and guide planes.
+// REF_EXACT: a 3-D map {texel, row, plane} over pass L's input (residue-major
+// planes of stride 2^L; 8-byte texels of fp16 images as UINT64, 16-byte ones as
+// 4 floats), box = one 36 x 20 halo tile of one plane.  A level whose plane
+// rows are not a multiple of 16 bytes stages with plain loads.
+void build_ref_maps(tg_svgf* s, EncodeTiledFn enc)
+{
+    const bool f16 = s->p.storage == TG_SVGF_STORAGE_FP16;
+    const uint64_t tb = f16 ? 8 : 16;
+    for (int lv = 1; lv < s->p.levels && lv < 10; ++lv) {
+        s->ref_lv_ok[lv] = false;
+        const ResLayout L = res_layout(int(s->w), int(s->h), lv);
+        if ((tb * L.pw) % 16 || (tb * L.pw * L.ph) % 16) continue;
+        void* base = (lv & 1) ? s->colB : s->colA;  // pass 1 reads col B, pass 2 col A, ...
+        const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
+        const cuuint64_t dim[3] = {f16 ? cuuint64_t(L.pw) : 4ull * L.pw, cuuint64_t(L.ph), planes};
+        const cuuint64_t str[2] = {tb * L.pw, tb * L.pw * L.ph};
+        const cuuint32_t box[3] = {f16 ? cuuint32_t(LevelTile<kLevelR>::SW) : 4u * LevelTile<kLevelR>::SW,
+                                   LevelTile<kLevelR>::SH, 1};
+        const cuuint32_t es[3] = {1, 1, 1};
+        const CUresult r = enc(&s->ref_lv[lv], f16 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                               base, dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        s->ref_lv_ok[lv] = r == CUDA_SUCCESS;
+    }
+}
+
+// REF_EXACT: the 2-D map over the caller's radiance {texel, row} (RGBA16F as
+// UINT64 texels, RGBA32F as 4 floats), re-encoded when the buffer, its pitch or
+// its format changes; false (plain loads) when TMA cannot address it.
+bool ref_input_map(tg_svgf* s, const tg_image& im)
+{
+    if (s->flags & TG_SVGF_FLAG_NO_TMA) return false;
+    const int64_t tb = im.format == TG_FMT_RGBA16F ? 8 : 16;
+    const int64_t pitch = im.pitch_bytes ? im.pitch_bytes : tb * int64_t(s->w);
+    if (s->ref_in_ok && s->ref_in_ptr == im.ptr && s->ref_in_pitch == pitch && s->ref_in_fmt == im.format) return true;
+    s->ref_in_ok = false;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || (reinterpret_cast<uintptr_t>(im.ptr) % 16) || pitch % 16) return false;
+    const bool h = tb == 8;
+    const cuuint64_t dim[2] = {h ? cuuint64_t(s->w) : 4ull * s->w, s->h};
+    const cuuint64_t str[1] = {cuuint64_t(pitch)};
+    const cuuint32_t box[2] = {h ? cuuint32_t(LevelTile<kLevelR>::SW) : 4u * LevelTile<kLevelR>::SW,
+                               LevelTile<kLevelR>::SH};
+    const cuuint32_t es[2] = {1, 1};
+    if (enc(&s->ref_in, h ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, im.ptr, dim, str, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    s->ref_in_ok = true;
+    s->ref_in_ptr = im.ptr;
+    s->ref_in_pitch = pitch;
+    s->ref_in_fmt = im.format;
+    return true;
+}
+
 void build_tensor_maps(tg_svgf* s)
 {
     s->tma = false;
-    if (s->p.mode != TG_SVGF_MODE_FULL || (s->flags & TG_SVGF_FLAG_NO_TMA)) return;
+    for (bool& ok : s->ref_lv_ok) ok = false;
+    s->ref_in_ok = false;
+    if (s->flags & TG_SVGF_FLAG_NO_TMA) return;
     EncodeTiledFn enc = encode_tiled();
     if (!enc) return;
+    if (s->p.mode == TG_SVGF_MODE_REF_EXACT) {
+        build_ref_maps(s, enc);
+        s->tma = true;  // interior tiles of the later passes (where their planes allow) and of the first pass
+        return;
+    }
     const bool f16 = s->p.storage == TG_SVGF_STORAGE_FP16;
     for (int lv = 1; lv < s->p.levels; ++lv) {
         const ResLayout L = res_layout(int(s->w), int(s->h), lv);
@@ -517,7 +588,12 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         const double rb = fmt_bytes(in->radiance.format), ob = fmt_bytes(out->denoised.format);
         const int levels = s->p.levels;
         int lv = 0;
-        enqueue_ref_chain<kLevelR>(a, s->colA, s->colB, levels, f16, stream, [&](bool first, auto body) {
+        a.err = s->d_err;
+        RefMaps maps;
+        if (ref_input_map(s, in->radiance)) maps.first = &s->ref_in;
+        for (int L = 1; L < levels && L < 10; ++L)
+            if (s->ref_lv_ok[L]) maps.level[L] = &s->ref_lv[L];
+        enqueue_ref_chain<kLevelR>(a, s->colA, s->colB, levels, f16, stream, maps, [&](bool first, auto body) {
             const bool last = lv == levels - 1;
             // compulsory bytes: the fused pass reads radiance and moments_prev and writes moments_curr; every
             // pass reads its input image and writes its output (the caller's image at the last pass)

@@ -56,6 +56,7 @@ struct RefArgs {
     float var_eps;        // VARIANCE_EPSILON
     int stride;
     int final_pass;
+    int* err;             // device error word of bounded waits (may be null)
 };
 
 // ------------------------------------------------------------------ FULL ----

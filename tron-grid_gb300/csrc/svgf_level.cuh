@@ -661,11 +661,66 @@ __device__ __forceinline__ void ref_taps_out(const RefArgs& a, int s, int ra, in
     }
 }
 
+// TMA staging of a REF_EXACT tile (interior tiles only: no clamping needed).
+// One thread issues the halo box of 8- or 16-byte texels into `land`; the
+// others wait (bounded), then each cell is converted into sA as
+// (r, g, b, luminance) of the colour rounded to the storage format.  Returns
+// false (every thread) if the box did not land in time, after recording the
+// timeout in a.err.
+template <int ST, int R>
+__device__ __forceinline__ bool ref_tma_land(const RefArgs& a, uint32_t ubar, bool f16_texels, const float4* land,
+                                             float4* sA)
+{
+    typedef LevelTile<R> T;
+    const int tid = threadIdx.y * kLvTX + threadIdx.x;
+    const bool landed = mbar_wait_bounded(ubar, 0);
+    if (__syncthreads_or(!landed)) {
+        if (tid == 0) {
+            if (a.err) atomicExch(a.err, 1);
+            mbar_wait_bounded(ubar, 0);  // give the copy a second bounded chance to retire
+        }
+        return false;
+    }
+    for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+        const float4 c = Stor<ST>::rt4(f16_texels ? unpack_h4(reinterpret_cast<const uint2*>(land)[k]) : land[k]);
+        sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
+    }
+    return true;
+}
+
+// Issues the box (one thread): `dims` 2 (x, row) or 3 (x, row, plane); x in
+// elements of the map (texels for 8-byte texels, floats for 16-byte ones).
+__device__ __forceinline__ void ref_tma_issue(const CUtensorMap* tm, uint32_t ubar, void* land, uint32_t bytes, int dims,
+                                              int x, int y, int z)
+{
+    const uint64_t map = reinterpret_cast<uint64_t>(tm);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(bytes) : "memory");
+    if (dims == 2)
+        asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                     "[%4];" ::"r"(smem_u32(land)),
+                     "l"(map), "r"(x), "r"(y), "r"(ubar)
+                     : "memory");
+    else
+        asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+                     "[%5];" ::"r"(smem_u32(land)),
+                     "l"(map), "r"(x), "r"(y), "r"(z), "r"(ubar)
+                     : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_cta(uint32_t ubar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // Init and the first wavelet pass (stride 1) in one kernel: reads the caller's
 // radiance and moments_prev, writes moments_curr and the pass's output (the
-// next pass's input, or the caller's image when it is the only pass).
-template <int ST, int R, bool IN>
-__device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0, float4* sA)
+// next pass's input, or the caller's image when it is the only pass).  TM: the
+// tile (interior) is staged by TMA from the caller's radiance through `tm`.
+template <int ST, int R, bool IN, bool TM>
+__device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0, float4* sA, const CUtensorMap* tm,
+                                               float4* land, uint32_t ubar)
 {
     typedef Stor<ST> S;
     typedef typename S::mom_t M;
@@ -684,16 +739,21 @@ __device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0,
         craw[k] = valid[k] ? ld_rgba(a.raw, x, y) : make_float4(0.f, 0.f, 0.f, 0.f);
         mp[k] = valid[k] ? S::ldm(static_cast<const M*>(a.mom_prev), size_t(y) * a.w + x) : make_float2(0.f, 0.f);
     }
-    for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
-        const int sj = k / T::SW, si = k - sj * T::SW;
-        int x = i0 + si - 2, y = j0 + sj - 2;
-        if (!IN) {
-            x = min(max(x, 0), a.w - 1);
-            y = min(max(y, 0), a.h - 1);
-        }
+    if constexpr (TM) {
         // wavelet_a's colour as the init pass stores it: the radiance in the storage format
-        const float4 c = S::rt4(ld_rgba(a.raw, x, y));
-        sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
+        if (!ref_tma_land<ST, R>(a, ubar, a.raw.fmt == TG_FMT_RGBA16F, land, sA)) return;
+    } else {
+        for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+            const int sj = k / T::SW, si = k - sj * T::SW;
+            int x = i0 + si - 2, y = j0 + sj - 2;
+            if (!IN) {
+                x = min(max(x, 0), a.w - 1);
+                y = min(max(y, 0), a.h - 1);
+            }
+            // wavelet_a's colour as the init pass stores it: the radiance in the storage format
+            const float4 c = S::rt4(ld_rgba(a.raw, x, y));
+            sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
+        }
     }
     // src/svgf_denoise.slang:177-190: moments EMA and sqrt-variance (the alpha wavelet_a would carry)
 #pragma unroll
@@ -717,21 +777,42 @@ __device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0,
     ref_taps_out<ST, R>(a, 1, 0, 0, i0, j0, ca, valid, sA);
 }
 
-template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref_first(RefArgs a, LevelGeom g)
+// use_tma: interior tiles are staged through `tm`, a 2-D map over the caller's
+// radiance ({8-byte texel, row} for RGBA16F, {float, row} for RGBA32F);
+// border tiles (clamped taps) and use_tma == 0 stage with plain loads.
+template <int ST, int R>
+__global__ void __launch_bounds__(kLvTX* kLvRows)
+    k_ref_first(RefArgs a, LevelGeom g, const __grid_constant__ CUtensorMap tm, int use_tma)
 {
     typedef LevelTile<R> T;
     __shared__ float4 sA[T::N];
+    __shared__ __align__(128) float4 land[T::N];
+    __shared__ __align__(8) uint64_t bar;
     const int i0 = int(blockIdx.x % unsigned(g.tiles_x)) * T::TX;
     const int j0 = int(blockIdx.x / unsigned(g.tiles_x)) * T::TY;
-    if (ref_tile_interior<R>(a.w, a.h, 1, 0, 0, i0, j0))
-        ref_first_tile<ST, R, true>(a, i0, j0, sA);
-    else
-        ref_first_tile<ST, R, false>(a, i0, j0, sA);
+    const bool in = ref_tile_interior<R>(a.w, a.h, 1, 0, 0, i0, j0);
+    if (in && use_tma) {
+        const uint32_t ubar = smem_u32(&bar);
+        if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init_cta(ubar);
+        __syncthreads();
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            const bool h = a.raw.fmt == TG_FMT_RGBA16F;
+            // x = i0 - 2 texels: even, so the box starts on a 16-byte boundary for 8-byte texels
+            ref_tma_issue(&tm, ubar, land, T::N * (h ? 8u : 16u), 2, h ? i0 - 2 : 4 * (i0 - 2), j0 - 2, 0);
+        }
+        ref_first_tile<ST, R, true, true>(a, i0, j0, sA, &tm, land, ubar);
+    } else if (in) {
+        ref_first_tile<ST, R, true, false>(a, i0, j0, sA, &tm, land, 0);
+    } else {
+        ref_first_tile<ST, R, false, false>(a, i0, j0, sA, &tm, land, 0);
+    }
 }
 
-// One wavelet pass at stride s >= 2 over residue-major scratch.
-template <int ST, int R, bool IN>
-__device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, int rb, int i0, int j0, float4* sA)
+// One wavelet pass at stride s >= 2 over residue-major scratch.  TM: the tile
+// (interior) is staged by TMA (the box already issued into `land`).
+template <int ST, int R, bool IN, bool TM>
+__device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, int rb, int i0, int j0, float4* sA,
+                                               const float4* land, uint32_t ubar)
 {
     typedef Stor<ST> S;
     typedef typename S::c4_t C4;
@@ -751,7 +832,9 @@ __device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, 
         valid[k] = IN || (x < a.w && y < a.h);
         ca[k] = valid[k] ? S::ld4_w(src, res_idx(a.lin, x, y)) : 0.f;
     }
-    if (IN) {
+    if constexpr (TM) {
+        if (!ref_tma_land<ST, R>(a, ubar, ST == ST_FP16, land, sA)) return;
+    } else if (IN) {
         // the tile's plane rows are contiguous runs of the residue-major layout
         const int base = ((rb << a.lin.lg) + ra) * a.lin.ph * pw + (j0 - 2) * pw + (i0 - 2);
         for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
@@ -772,16 +855,36 @@ __device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, 
     ref_taps_out<ST, R>(a, s, ra, rb, i0, j0, ca, valid, sA);
 }
 
-template <int ST, int R> __global__ void __launch_bounds__(kLvTX* kLvRows) k_ref_level(RefArgs a, LevelGeom g)
+// use_tma: interior tiles are staged through `tm`, a 3-D map over the input's
+// residue planes ({8-byte texel, row, plane} for fp16 images, {float, row,
+// plane} for fp32 ones); border tiles and use_tma == 0 stage with plain loads.
+template <int ST, int R>
+__global__ void __launch_bounds__(kLvTX* kLvRows)
+    k_ref_level(RefArgs a, LevelGeom g, const __grid_constant__ CUtensorMap tm, int use_tma)
 {
     typedef LevelTile<R> T;
     __shared__ float4 sA[T::N];
+    __shared__ __align__(128) float4 land[T::N];
+    __shared__ __align__(8) uint64_t bar;
     int ra, rb, i0, j0;
     level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
-    if (ref_tile_interior<R>(a.w, a.h, g.s, ra, rb, i0, j0))
-        ref_level_tile<ST, R, true>(a, g.s, ra, rb, i0, j0, sA);
-    else
-        ref_level_tile<ST, R, false>(a, g.s, ra, rb, i0, j0, sA);
+    const bool in = ref_tile_interior<R>(a.w, a.h, g.s, ra, rb, i0, j0);
+    if (in && use_tma) {
+        const uint32_t ubar = smem_u32(&bar);
+        if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init_cta(ubar);
+        __syncthreads();
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            constexpr bool h = ST == ST_FP16;
+            // x = i0 - 2 texels: even, so the box starts on a 16-byte boundary for 8-byte texels
+            ref_tma_issue(&tm, ubar, land, T::N * (h ? 8u : 16u), 3, h ? i0 - 2 : 4 * (i0 - 2), j0 - 2,
+                          (rb << g.lg) + ra);
+        }
+        ref_level_tile<ST, R, true, true>(a, g.s, ra, rb, i0, j0, sA, land, ubar);
+    } else if (in) {
+        ref_level_tile<ST, R, true, false>(a, g.s, ra, rb, i0, j0, sA, land, 0);
+    } else {
+        ref_level_tile<ST, R, false, false>(a, g.s, ra, rb, i0, j0, sA, land, 0);
+    }
 }
 
 __host__ __device__ inline LevelGeom level_geom(int w, int h, int s, int R)
@@ -802,15 +905,24 @@ __host__ __device__ inline unsigned level_blocks(const LevelGeom& g)
     return unsigned(g.s * g.s) * g.tiles_x * g.tiles_y;
 }
 
+// Tensor maps for TMA staging of the REF_EXACT chain (null: plain loads).
+// first: over the caller's radiance; level[L]: over pass L's input planes.
+struct RefMaps {
+    const CUtensorMap* first = nullptr;
+    const CUtensorMap* level[10] = {};
+};
+
 // Enqueues one REF_EXACT frame on `stream`: the init fused into the first pass
 // (stride 1, output to `wb`), then passes at strides 2, 4, ... alternating
 // wb -> wa -> wb; the last pass writes the caller's image.  `a` carries the
 // images and constants.  hook(first, body) runs each launch body (first: the
 // fused pass), so that a caller can bracket it with events.
 template <int R, class Hook>
-void enqueue_ref_chain(RefArgs a, void* wa, void* wb, int levels, bool f16, cudaStream_t stream, Hook hook)
+void enqueue_ref_chain(RefArgs a, void* wa, void* wb, int levels, bool f16, cudaStream_t stream, const RefMaps& maps,
+                       Hook hook)
 {
     const dim3 blk(kLvTX, kLvRows);
+    const CUtensorMap none{};
     a.src = nullptr;
     a.dst = wb;
     a.stride = 1;
@@ -819,10 +931,12 @@ void enqueue_ref_chain(RefArgs a, void* wa, void* wb, int levels, bool f16, cuda
     a.lout = res_layout(a.w, a.h, 1);
     const LevelGeom g0 = level_geom(a.w, a.h, 1, R);
     hook(true, [&] {
+        const CUtensorMap& m = maps.first ? *maps.first : none;
+        const int t = maps.first != nullptr;
         if (f16)
-            k_ref_first<ST_FP16, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0);
+            k_ref_first<ST_FP16, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0, m, t);
         else
-            k_ref_first<ST_FP32, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0);
+            k_ref_first<ST_FP32, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0, m, t);
     });
     void* src = wb;
     void* oth = wa;
@@ -835,10 +949,12 @@ void enqueue_ref_chain(RefArgs a, void* wa, void* wb, int levels, bool f16, cuda
         a.lout = res_layout(a.w, a.h, lv + 1);
         const LevelGeom g = level_geom(a.w, a.h, a.stride, R);
         hook(false, [&] {
+            const CUtensorMap& m = maps.level[lv] ? *maps.level[lv] : none;
+            const int t = maps.level[lv] != nullptr;
             if (f16)
-                k_ref_level<ST_FP16, R><<<level_blocks(g), blk, 0, stream>>>(a, g);
+                k_ref_level<ST_FP16, R><<<level_blocks(g), blk, 0, stream>>>(a, g, m, t);
             else
-                k_ref_level<ST_FP32, R><<<level_blocks(g), blk, 0, stream>>>(a, g);
+                k_ref_level<ST_FP32, R><<<level_blocks(g), blk, 0, stream>>>(a, g, m, t);
         });
         void* t = src;
         src = oth;

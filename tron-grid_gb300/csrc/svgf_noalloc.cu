@@ -161,7 +161,9 @@ extern "C" int tg_svgf_denoise_ref_noalloc(const tg_svgf_params* params, uint32_
     a.phi = params->sigma_l;
     a.alpha_m = params->moments_alpha;
     a.var_eps = params->variance_epsilon;
-    enqueue_ref_chain<2>(a, wa, wb, params->levels, f16, stream, [](bool, auto body) { body(); });
+    // plain staging (no tensor maps): TMA's bounded waits report through a device error word this entry point
+    // does not have
+    enqueue_ref_chain<2>(a, wa, wb, params->levels, f16, stream, RefMaps{}, [](bool, auto body) { body(); });
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TG_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
     return TG_OK;
