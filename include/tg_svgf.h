@@ -340,7 +340,11 @@ typedef struct tg_svgf_server_stats {
 TG_API int tg_svgf_server_create(const tg_svgf_server_desc* desc, tg_svgf_server** out);
 
 /* Queues one frame of `session` (width x height; host inputs/outputs, kept
- * alive and unmodified until the ticket completes; pinned for overlap). */
+ * alive and unmodified until the ticket completes).  Inputs in page-locked
+ * host memory mapped for the device (cudaHostAlloc, cudaHostRegister; e.g.
+ * torch pin_memory) are read by the kernels in place over the host link, with
+ * no copy; other host inputs are copied into device slots.  Outputs are copied
+ * out (page-locked outputs overlap with the next launches). */
 TG_API int tg_svgf_server_submit(tg_svgf_server* s, uint64_t session, uint32_t width, uint32_t height,
                                  const tg_svgf_inputs* host_inputs, const tg_svgf_outputs* host_outputs,
                                  uint64_t* ticket);

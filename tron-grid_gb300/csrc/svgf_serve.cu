@@ -124,6 +124,7 @@ struct Sess {
     char* state;
     size_t state_len;
     char* in_slot[2][4];
+    tg_image in_view[4];  // the current frame's inputs as the kernels read them (a slot, or mapped host memory)
     char* out_slot[2];
     uint64_t frames = 0, lru = 0;
     int pending = 0;  // queued + running frames
@@ -283,7 +284,7 @@ FullArgs args_for(tg_svgf_server* sv, Sess& s)
     a.h = int(s.h);
     const int slot = cur;
     tg_image im[5];
-    for (int k = 0; k < 4; ++k) im[k] = tg_image{s.in_slot[slot][k], 0, s.fmt[k], 0};
+    for (int k = 0; k < 4; ++k) im[k] = s.in_view[k];
     im[4] = tg_image{s.out_slot[slot], 0, s.fmt[4], 0};
     a.radiance = to_img(im[0], s.w);
     a.depth = to_img(im[1], s.w);
@@ -457,6 +458,21 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
     }
 }
 
+// Device address at which the GPU reads host memory `p` in place: page-locked
+// memory mapped into the device's address space (cudaHostAlloc,
+// cudaHostRegister) on this server's device; null for anything else (pageable
+// memory, device memory), which is copied in instead.
+void* mapped_view(const tg_svgf_server* sv, const void* p)
+{
+    cudaPointerAttributes at;
+    if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer || at.device != sv->device) return nullptr;
+    return at.devicePointer;
+}
+
 // A completion event from the pool (created when the pool is empty); the
 // caller holds sv->mu.
 cudaEvent_t pool_event(tg_svgf_server* sv)
@@ -575,7 +591,10 @@ void scheduler(tg_svgf_server* sv)
         }
         if (failed_any) sv->cv_done.notify_all();
         const int k = batch_no % kMaxInflight;
-        // inputs in (copy stream); slots alternate by frame parity
+        // Inputs: page-locked, mapped host images are read by the temporal kernel in place over the host link
+        // (no copy, no API call per image); others are copied into the session's slot on the copy stream
+        // (slots alternate by frame parity).
+        bool copied = false;
         for (size_t j = 0; j < batch.size(); ++j) {
             Req* r = batch[j];
             Sess& s = *ss[j];
@@ -584,12 +603,20 @@ void scheduler(tg_svgf_server* sv)
             for (int q = 0; q < 4; ++q) {
                 const size_t row = size_t(fmt_bytes(s.fmt[q])) * s.w;
                 const size_t hp = src[q]->pitch_bytes ? size_t(src[q]->pitch_bytes) : row;
+                if (void* dv = mapped_view(sv, src[q]->ptr)) {
+                    s.in_view[q] = tg_image{dv, int64_t(hp), s.fmt[q], 0};
+                    continue;
+                }
                 cudaMemcpy2DAsync(s.in_slot[slot][q], row, src[q]->ptr, hp, row, s.h, cudaMemcpyHostToDevice,
                                   sv->s_h2d);
+                s.in_view[q] = tg_image{s.in_slot[slot][q], 0, s.fmt[q], 0};
+                copied = true;
             }
         }
-        cudaEventRecord(sv->ev_h2d, sv->s_h2d);
-        cudaStreamWaitEvent(sv->s_comp, sv->ev_h2d, 0);
+        if (copied) {
+            cudaEventRecord(sv->ev_h2d, sv->s_h2d);
+            cudaStreamWaitEvent(sv->s_comp, sv->ev_h2d, 0);
+        }
         for (Sess* s : fresh) cudaMemsetAsync(s->state, 0, s->state_len, sv->s_comp);
         Flight* fl = new Flight();
         fl->reqs = batch;
