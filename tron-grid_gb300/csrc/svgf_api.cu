@@ -192,8 +192,13 @@ int validate_params(const tg_svgf_params& p)
 } // namespace tg
 
 namespace tg {
-// Output rows per thread of the tiled a-trous kernels.
+// Output rows per thread of the tiled a-trous kernels: FULL (kLevelR) and
+// REF_EXACT (kRefR).
 constexpr int kLevelR = 2;
+#ifndef TG_REF_R
+#define TG_REF_R 2
+#endif
+constexpr int kRefR = TG_REF_R;
 
 typedef void (*LevelTmaFn)(FullArgs, LevelArgs, LevelGeom, const CUtensorMap, const CUtensorMap);
 typedef void (*LevelTiledFn)(FullArgs, LevelGeom);
@@ -366,8 +371,8 @@ void build_ref_maps(tg_svgf* s, EncodeTiledFn enc)
         const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
         const cuuint64_t dim[3] = {f16 ? cuuint64_t(L.pw) : 4ull * L.pw, cuuint64_t(L.ph), planes};
         const cuuint64_t str[2] = {tb * L.pw, tb * L.pw * L.ph};
-        const cuuint32_t box[3] = {f16 ? cuuint32_t(LevelTile<kLevelR>::SW) : 4u * LevelTile<kLevelR>::SW,
-                                   LevelTile<kLevelR>::SH, 1};
+        const cuuint32_t box[3] = {f16 ? cuuint32_t(LevelTile<kRefR>::SW) : 4u * LevelTile<kRefR>::SW,
+                                   LevelTile<kRefR>::SH, 1};
         const cuuint32_t es[3] = {1, 1, 1};
         const CUresult r = enc(&s->ref_lv[lv], f16 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                                base, dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -391,8 +396,8 @@ bool ref_input_map(tg_svgf* s, const tg_image& im)
     const bool h = tb == 8;
     const cuuint64_t dim[2] = {h ? cuuint64_t(s->w) : 4ull * s->w, s->h};
     const cuuint64_t str[1] = {cuuint64_t(pitch)};
-    const cuuint32_t box[2] = {h ? cuuint32_t(LevelTile<kLevelR>::SW) : 4u * LevelTile<kLevelR>::SW,
-                               LevelTile<kLevelR>::SH};
+    const cuuint32_t box[2] = {h ? cuuint32_t(LevelTile<kRefR>::SW) : 4u * LevelTile<kRefR>::SW,
+                               LevelTile<kRefR>::SH};
     const cuuint32_t es[2] = {1, 1};
     if (enc(&s->ref_in, h ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, im.ptr, dim, str, box,
             es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -593,7 +598,7 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         if (ref_input_map(s, in->radiance)) maps.first = &s->ref_in;
         for (int L = 1; L < levels && L < 10; ++L)
             if (s->ref_lv_ok[L]) maps.level[L] = &s->ref_lv[L];
-        enqueue_ref_chain<kLevelR>(a, s->colA, s->colB, levels, f16, stream, maps, [&](bool first, auto body) {
+        enqueue_ref_chain<kRefR>(a, s->colA, s->colB, levels, f16, stream, maps, [&](bool first, auto body) {
             const bool last = lv == levels - 1;
             // compulsory bytes: the fused pass reads radiance and moments_prev and writes moments_curr; every
             // pass reads its input image and writes its output (the caller's image at the last pass)

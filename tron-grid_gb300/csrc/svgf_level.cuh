@@ -777,11 +777,18 @@ __device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0,
     ref_taps_out<ST, R>(a, 1, 0, 0, i0, j0, ca, valid, sA);
 }
 
+// CTAs per SM the REF_EXACT kernels are compiled for: 6 (40 registers a
+// thread, 48 warps) measured 14% faster per 4K frame than the 5 that 42
+// registers allowed; 3 rows per thread (28 rows staged per 24) was slower.
+#ifndef TG_REF_CTAS
+#define TG_REF_CTAS 6
+#endif
+
 // use_tma: interior tiles are staged through `tm`, a 2-D map over the caller's
 // radiance ({8-byte texel, row} for RGBA16F, {float, row} for RGBA32F);
 // border tiles (clamped taps) and use_tma == 0 stage with plain loads.
 template <int ST, int R>
-__global__ void __launch_bounds__(kLvTX* kLvRows)
+__global__ void __launch_bounds__(kLvTX* kLvRows, TG_REF_CTAS)
     k_ref_first(RefArgs a, LevelGeom g, const __grid_constant__ CUtensorMap tm, int use_tma)
 {
     typedef LevelTile<R> T;
@@ -859,7 +866,7 @@ __device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, 
 // residue planes ({8-byte texel, row, plane} for fp16 images, {float, row,
 // plane} for fp32 ones); border tiles and use_tma == 0 stage with plain loads.
 template <int ST, int R>
-__global__ void __launch_bounds__(kLvTX* kLvRows)
+__global__ void __launch_bounds__(kLvTX* kLvRows, TG_REF_CTAS)
     k_ref_level(RefArgs a, LevelGeom g, const __grid_constant__ CUtensorMap tm, int use_tma)
 {
     typedef LevelTile<R> T;
