@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 KEYS = ("radiance", "depth", "normal", "motion")
 
 
-def _host_seq(w, h, frames, seed, f16=False):
+def _host_seq(w, h, frames, seed, f16=False, pinned=True):
     sc = scene.PlaneScene(scene.config1(w, h, seed=seed))
     seq = []
     for t in range(frames):
@@ -22,7 +22,7 @@ def _host_seq(w, h, frames, seed, f16=False):
         if f16:
             d["radiance"] = d["radiance"].half()
             d["normal"] = torch.from_numpy(oracle.oct16_encode(fr["normal"].numpy()))
-        seq.append({k: v.contiguous().pin_memory() for k, v in d.items()})
+        seq.append({k: (v.contiguous().pin_memory() if pinned else v.contiguous().clone()) for k, v in d.items()})
     return seq
 
 
@@ -38,12 +38,15 @@ def _single(w, h, seq, storage, dev):
     return outs
 
 
-@pytest.mark.parametrize("batching,strategy", [(True, 0), (True, 1), (False, 0)])
-def test_sessions_alone_equal_in_mix(cuda_dev, batching, strategy):
-    """Interleaved frames of several sessions give each session the single-stream result."""
+@pytest.mark.parametrize("batching,strategy,pinned", [(True, 0, True), (True, 1, True), (False, 0, True),
+                                                      (True, 0, False), (False, 0, False)])
+def test_sessions_alone_equal_in_mix(cuda_dev, batching, strategy, pinned):
+    """Interleaved frames of several sessions give each session the single-stream result, whether the launch
+    that carries a frame holds one frame (single-stream kernels) or several (batched kernels), and whether its
+    inputs are read in place from page-locked host memory (pinned) or copied in (pageable)."""
     sizes = [(64, 36), (160, 90), (33, 17)]
     frames = 4
-    seqs = [_host_seq(w, h, frames, seed=3 + j, f16=True) for j, (w, h) in enumerate(sizes)]
+    seqs = [_host_seq(w, h, frames, seed=3 + j, f16=True, pinned=pinned) for j, (w, h) in enumerate(sizes)]
     want = [_single(w, h, seq, tg.STORAGE_FP16, cuda_dev) for (w, h), seq in zip(sizes, seqs)]
     sv = Server(256 << 20, max_batch=8, batching=batching, storage=tg.STORAGE_FP16, strategy=strategy)
     outs = [[torch.empty((h, w, 4), dtype=torch.float16, pin_memory=True) for _ in range(frames)] for (w, h) in sizes]

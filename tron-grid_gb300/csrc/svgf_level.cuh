@@ -652,7 +652,8 @@ __device__ __forceinline__ void ref_taps_out(const RefArgs& a, int s, int ra, in
             o = make_float4(c.x, c.y, c.z, ca[k]);
         }
         if (a.final_pass) {
-            if (ST == ST_FP16) o = make_float4(q16(o.x), q16(o.y), q16(o.z), 1.0f);
+            // fp16 images round to binary16 (an RGBA16F output's store does the same rounding itself)
+            if (ST == ST_FP16 && a.out.fmt != TG_FMT_RGBA16F) o = make_float4(q16(o.x), q16(o.y), q16(o.z), 1.0f);
             o.w = 1.0f;
             st_rgba(a.out, x, y, o);
         } else {
@@ -681,7 +682,11 @@ __device__ __forceinline__ bool ref_tma_land(const RefArgs& a, uint32_t ubar, bo
         }
         return false;
     }
-    for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
+    constexpr int kThreads = kLvTX * kLvRows;
+#pragma unroll
+    for (int e = 0; e < (T::N + kThreads - 1) / kThreads; ++e) {
+        const int k = tid + e * kThreads;
+        if (k >= T::N) break;
         const float4 c = Stor<ST>::rt4(f16_texels ? unpack_h4(reinterpret_cast<const uint2*>(land)[k]) : land[k]);
         sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
     }
@@ -830,6 +835,7 @@ __device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, 
     const int pw = a.lin.pw;
     // each centre's alpha (the sigma of its luminance weight), loaded before the staging so that its latency
     // overlaps it
+    // (a TMA-staged tile takes them from the landed texels instead)
     float ca[R];
     bool valid[R];
 #pragma unroll
@@ -837,10 +843,15 @@ __device__ __forceinline__ void ref_level_tile(const RefArgs& a, int s, int ra, 
         const int x = ra + s * (i0 + ci);
         const int y = rb + s * (j0 + cj0 + k);
         valid[k] = IN || (x < a.w && y < a.h);
-        ca[k] = valid[k] ? S::ld4_w(src, res_idx(a.lin, x, y)) : 0.f;
+        ca[k] = (!TM && valid[k]) ? S::ld4_w(src, res_idx(a.lin, x, y)) : 0.f;
     }
     if constexpr (TM) {
         if (!ref_tma_land<ST, R>(a, ubar, ST == ST_FP16, land, sA)) return;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int c = (cj0 + k + 2) * T::SW + ci + 2;
+            ca[k] = ST == ST_FP16 ? unpack_h2(reinterpret_cast<const uint2*>(land)[c].y).y : land[c].w;
+        }
     } else if (IN) {
         // the tile's plane rows are contiguous runs of the residue-major layout
         const int base = ((rb << a.lin.lg) + ra) * a.lin.ph * pw + (j0 - 2) * pw + (i0 - 2);

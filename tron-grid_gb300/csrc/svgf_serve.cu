@@ -621,14 +621,17 @@ void scheduler(tg_svgf_server* sv)
         Flight* fl = new Flight();
         fl->reqs = batch;
         fl->sess = ss;
-        fl->table_k = (sv->d.batching && sv->d.strategy == TG_SVGF_BATCH_PERSISTENT) ? k : -1;
+        // a launch of one frame runs the single-stream kernels (no work table to copy or search); two or more run
+        // the batched kernels, whose results are bit-identical
+        const bool batched = sv->d.batching && batch.size() > 1;
+        fl->table_k = (batched && sv->d.strategy == TG_SVGF_BATCH_PERSISTENT) ? k : -1;
         {
             std::lock_guard<std::mutex> lk(sv->mu);
             fl->ev_comp = pool_event(sv);
             fl->ev_d2h = pool_event(sv);
         }
         const Clock::time_point tl = Clock::now();
-        if (sv->d.batching)
+        if (batched)
             launch_batch(sv, ss, k);
         else
             launch_plain(sv, *ss[0]);
