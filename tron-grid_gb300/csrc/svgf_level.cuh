@@ -737,16 +737,23 @@ __device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0,
     float4 craw[R];
     float2 mp[R];
     // each centre's radiance and previous moments, loaded before the staging so that their latency overlaps it
+    // (a TMA-staged tile takes the radiance from the landed texels instead)
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int x = i0 + ci, y = j0 + cj0 + k;
         valid[k] = IN || (x < a.w && y < a.h);
-        craw[k] = valid[k] ? ld_rgba(a.raw, x, y) : make_float4(0.f, 0.f, 0.f, 0.f);
+        craw[k] = (!TM && valid[k]) ? ld_rgba(a.raw, x, y) : make_float4(0.f, 0.f, 0.f, 0.f);
         mp[k] = valid[k] ? S::ldm(static_cast<const M*>(a.mom_prev), size_t(y) * a.w + x) : make_float2(0.f, 0.f);
     }
     if constexpr (TM) {
         // wavelet_a's colour as the init pass stores it: the radiance in the storage format
-        if (!ref_tma_land<ST, R>(a, ubar, a.raw.fmt == TG_FMT_RGBA16F, land, sA)) return;
+        const bool h = a.raw.fmt == TG_FMT_RGBA16F;
+        if (!ref_tma_land<ST, R>(a, ubar, h, land, sA)) return;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int c = (cj0 + k + 2) * T::SW + ci + 2;
+            craw[k] = h ? unpack_h4(reinterpret_cast<const uint2*>(land)[c]) : land[c];
+        }
     } else {
         for (int k = tid; k < T::N; k += kLvTX * kLvRows) {
             const int sj = k / T::SW, si = k - sj * T::SW;
