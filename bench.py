@@ -391,33 +391,37 @@ def run_single(args, dev, mode_s, storage_s, steps, size=None):
     storage = tg.STORAGE_FP32 if storage_s == "fp32" else tg.STORAGE_FP16
     dt = torch.float32 if storage_s == "fp32" else torch.float16
     out = torch.empty((H, W, 4), dtype=dt, device=dev)
-    den = tg.Denoiser(W, H, mode=mode, storage=storage, device=dev.index)
     stream = torch.cuda.current_stream()
 
-    def step(i):
-        fr = frames[i % len(frames)]
-        den.denoise(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=out)
+    def run(profile):
+        """Frames 5 .. 5+steps-1 of the sequence after frames 0..4 on a fresh stream state: (ms per frame, the
+        library's per-kernel profile or None)."""
+        den = tg.Denoiser(W, H, mode=mode, storage=storage, device=dev.index)
 
-    for i in range(5):
-        step(i)
-    torch.cuda.synchronize()
-    # frames/s from a pass without the library's per-kernel events (on a chain of ~0.1 ms kernels their records
-    # cost several percent), then the per-kernel breakdown from a second, profiled pass over the same frames
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for i in range(steps):
-        step(5 + i)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    den.profile(True)
-    den.profile_read(reset=True)
-    for i in range(steps):
-        step(5 + i)
-    torch.cuda.synchronize()
-    prof = den.profile_read(reset=True)
-    den.profile(False)
-    den.close()
+        def step(i):
+            fr = frames[i % len(frames)]
+            den.denoise(fr["radiance"], fr.get("depth"), fr.get("normal"), fr.get("motion"), out=out)
+
+        for i in range(5):
+            step(i)
+        torch.cuda.synchronize()
+        if profile:
+            den.profile(True)
+            den.profile_read(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps):
+            step(5 + i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        prof = den.profile_read(reset=True) if profile else None
+        den.close()
+        return e0.elapsed_time(e1) / steps, prof
+
+    # frames/s from a run without the library's per-kernel events (on a chain of ~0.1 ms kernels their records
+    # cost several percent), the per-kernel breakdown from a second, profiled run over the same frames
+    ms, _ = run(False)
+    _, prof = run(True)
     bpp = algo_bytes_per_px(mode_s, storage_s)
     peak, _ = load_peaks()
     return {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "mpx_per_s": W * H / ms / 1e3,
