@@ -795,12 +795,15 @@ __device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0,
 #ifndef TG_REF_CTAS
 #define TG_REF_CTAS 6
 #endif
+#ifndef TG_REF_FIRST_CTAS
+#define TG_REF_FIRST_CTAS TG_REF_CTAS
+#endif
 
 // use_tma: interior tiles are staged through `tm`, a 2-D map over the caller's
 // radiance ({8-byte texel, row} for RGBA16F, {float, row} for RGBA32F);
 // border tiles (clamped taps) and use_tma == 0 stage with plain loads.
 template <int ST, int R>
-__global__ void __launch_bounds__(kLvTX* kLvRows, TG_REF_CTAS)
+__global__ void __launch_bounds__(kLvTX* kLvRows, TG_REF_FIRST_CTAS)
     k_ref_first(RefArgs a, LevelGeom g, const __grid_constant__ CUtensorMap tm, int use_tma)
 {
     typedef LevelTile<R> T;
