@@ -423,49 +423,19 @@ void build_tensor_maps(tg_svgf* s)
         s->tma = true;  // interior tiles of the later passes (where their planes allow) and of the first pass
         return;
     }
-    const bool f16 = s->p.storage == TG_SVGF_STORAGE_FP16;
+    CUtensorMap maps[kFullMaps];
+    const unsigned m = full_level_maps(s->p, s->w, s->h, kLevelR, s->colA, s->colB, s->tc, s->guide[0], s->guide[1], maps);
     for (int lv = 1; lv < s->p.levels; ++lv) {
-        const ResLayout L = res_layout(int(s->w), int(s->h), lv);
-        void* base = (lv & 1) ? s->colB : s->colA;
-        const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
-        // a row of either half-plane as 4 pw floats: one contiguous 576-byte line per tile row and half
-        const cuuint64_t dim[4] = {4ull * L.pw, cuuint64_t(L.ph), planes, 2};
-        const cuuint64_t str[3] = {16ull * L.pw, 16ull * L.pw * L.ph, 16ull * col_guide_half_of(s->p, s->w, s->h)};
-        const cuuint32_t box[4] = {4 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH, 1, 1};
-        const cuuint32_t es[4] = {1, 1, 1, 1};
-        const CUresult r = enc(&s->tmaps[lv], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dim, str, box, es,
-                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return;
+        if (!((m >> lv) & 1u)) return;
+        s->tmaps[lv] = maps[2 + lv];
     }
     s->tma = true;
-    // Level 0's planes: FP32 {float, row}, FP16 {8-byte texel, row} (its row pitch must be a multiple of 16 bytes,
-    // so an odd width stages level 0 with plain loads); each tile row is one contiguous line.
-    s->tma0 = false;
-    void* planes[3] = {s->tc, s->guide[0], s->guide[1]};
-    CUtensorMap* maps[3] = {&s->tm_tc, &s->tm_guide[0], &s->tm_guide[1]};
-    for (int k = 0; k < 3; ++k) {
-        CUresult r;
-        if (f16) {
-            if ((8ull * s->w) % 16) return;
-            const cuuint64_t dim[2] = {s->w, s->h};
-            const cuuint64_t str[1] = {8ull * s->w};
-            const cuuint32_t box[2] = {LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH};
-            const cuuint32_t es[2] = {1, 1};
-            r = enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, planes[k], dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        } else {
-            const cuuint64_t dim[2] = {4ull * s->w, s->h};
-            const cuuint64_t str[1] = {16ull * s->w};
-            const cuuint32_t box[2] = {4 * LevelTile<kLevelR>::SW, LevelTile<kLevelR>::SH};
-            const cuuint32_t es[2] = {1, 1};
-            r = enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, planes[k], dim, str, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        }
-        if (r != CUDA_SUCCESS) return;
+    s->tma0 = m & 1u;
+    if (s->tma0) {
+        s->tm_tc = maps[0];
+        s->tm_guide[0] = maps[1];
+        s->tm_guide[1] = maps[2];
     }
-    s->tma0 = true;
 }
 
 void free_buffers(tg_svgf* s)
@@ -537,6 +507,62 @@ int check_inputs(const tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outpu
 } // namespace
 
 namespace tg {
+
+// TMA maps of a FULL stream's a-trous levels for tiles of R output rows per
+// thread (box = 36 x (8R + 4) cells); see svgf_internal.h for the layout and
+// the mask.  Each map's preconditions (16-byte strides and base) are those of
+// cuTensorMapEncodeTiled; a level whose map cannot be encoded stages with plain
+// loads.
+unsigned full_level_maps(const tg_svgf_params& p, uint32_t w, uint32_t h, int R, void* colA, void* colB, void* tc,
+                         void* guide0, void* guide1, CUtensorMap* maps)
+{
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || p.mode != TG_SVGF_MODE_FULL) return 0;
+    const cuuint32_t SW = kLvTX + 4, SH = kLvRows * R + 4;
+    const bool f16 = p.storage == TG_SVGF_STORAGE_FP16;
+    unsigned mask = 0;
+    for (int lv = 1; lv < p.levels && 2 + lv < kFullMaps; ++lv) {
+        const ResLayout L = res_layout(int(w), int(h), lv);
+        void* base = (lv & 1) ? colB : colA;  // level L reads the records level L-1 wrote
+        const cuuint64_t planes = cuuint64_t(1) << (2 * lv);
+        // a row of either half-plane as 4 pw floats: one contiguous line per tile row and half
+        const cuuint64_t dim[4] = {4ull * L.pw, cuuint64_t(L.ph), planes, 2};
+        const cuuint64_t str[3] = {16ull * L.pw, 16ull * L.pw * L.ph, 16ull * col_guide_half_of(p, w, h)};
+        const cuuint32_t box[4] = {4 * SW, SH, 1, 1};
+        const cuuint32_t es[4] = {1, 1, 1, 1};
+        if (enc(&maps[2 + lv], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dim, str, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+            mask |= 1u << lv;
+    }
+    // Level 0's planes: FP32 {float, row}, FP16 {8-byte texel, row} (its row pitch must be a multiple of 16 bytes,
+    // so an odd width stages level 0 with plain loads); each tile row is one contiguous line.
+    if (f16 && (8ull * w) % 16) return mask;
+    void* planes[3] = {tc, guide0, guide1};
+    for (int k = 0; k < 3; ++k) {
+        CUresult r;
+        if (f16) {
+            const cuuint64_t dim[2] = {w, h};
+            const cuuint64_t str[1] = {8ull * w};
+            const cuuint32_t box[2] = {SW, SH};
+            const cuuint32_t es[2] = {1, 1};
+            r = enc(&maps[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, planes[k], dim, str, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        } else {
+            const cuuint64_t dim[2] = {4ull * w, h};
+            const cuuint64_t str[1] = {16ull * w};
+            const cuuint32_t box[2] = {4 * SW, SH};
+            const cuuint32_t es[2] = {1, 1};
+            r = enc(&maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, planes[k], dim, str, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        }
+        if (r != CUDA_SUCCESS) return mask;
+    }
+    return mask | 1u;
+}
+
 
 static cudaEvent_t prof_event(tg_svgf* s)
 {

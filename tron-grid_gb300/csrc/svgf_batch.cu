@@ -65,6 +65,10 @@ struct tg_svgf_batch {
     int strategy = TG_SVGF_BATCH_STAGES;
     std::vector<int> grids[2];  // per-stage grid of the step in table buffer k
     std::vector<int> sig[2];    // grids the graph of buffer k was captured with
+    // TMA maps of every stream's levels for tiles of 1 and of 2 rows per thread (kFullMaps per stream, built
+    // once: the streams' buffers never move), and which levels of each stream have them
+    CUtensorMap* d_maps[2] = {nullptr, nullptr};
+    std::vector<unsigned> tma_mask[2];
 };
 
 namespace {
@@ -299,6 +303,12 @@ void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const 
         a.fallback_frames = b->p.fallback_frames;
         ent[j].colA = s.colA;
         ent[j].colB = s.colB;
+        const int r = b->R == 1 ? 0 : 1;
+        if (b->d_maps[r]) {
+            ent[j].maps = b->d_maps[r] + size_t(kFullMaps) * ids[j];
+            ent[j].tma_mask = b->tma_mask[r][ids[j]];
+            ent[j].guide_k = cur;
+        }
         s.frames++;
     }
 }
@@ -350,7 +360,34 @@ void free_batch(tg_svgf_batch* b)
     if (b->h_err) cudaFreeHost(b->h_err);
     if (b->d_bar) cudaFree(b->d_bar);
     if (b->arena) cudaFree(b->arena);
+    for (auto& m : b->d_maps)
+        if (m) cudaFree(m);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+}
+
+// Encodes every stream's level maps for 1 and 2 rows per thread and copies them to the device; a batch whose
+// maps cannot be built (no encoder, no memory) stages every level with plain loads.
+void build_batch_maps(tg_svgf_batch* b)
+{
+    std::vector<CUtensorMap> h(size_t(kFullMaps) * b->n);
+    for (int r = 0; r < 2; ++r) {
+        b->tma_mask[r].assign(b->n, 0u);
+        unsigned any = 0;
+        for (int j = 0; j < b->n; ++j) {
+            const tg_svgf_batch::Stream& s = b->st[j];
+            b->tma_mask[r][j] = full_level_maps(b->p, b->w[j], b->h[j], r + 1, s.colA, s.colB, s.tc, s.guide[0],
+                                                s.guide[1], &h[size_t(kFullMaps) * j]);
+            any |= b->tma_mask[r][j];
+        }
+        if (!any) continue;
+        const size_t bytes = h.size() * sizeof(CUtensorMap);
+        if (cudaMalloc(&b->d_maps[r], bytes) != cudaSuccess ||
+            cudaMemcpy(b->d_maps[r], h.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            if (b->d_maps[r]) cudaFree(b->d_maps[r]);
+            b->d_maps[r] = nullptr;
+        }
+    }
 }
 
 } // namespace
@@ -444,6 +481,7 @@ int tg_svgf_batch_create(const tg_svgf_batch_desc* d, tg_svgf_batch** out)
         s.frames = 0;
     }
     if (cudaMemset(b->arena, 0, off[b->n]) != cudaSuccess) return cleanup(fail(TG_ERR_CUDA, "arena clear failed"));
+    build_batch_maps(b);
     b->cap = b->n;
     b->tbytes = table_bytes(b->cap);
     for (int k = 0; k < 2; ++k) {

@@ -37,6 +37,12 @@ struct BatchEntry {
     FullArgs fa;  // stream-level arguments (col_dst = colA for the variance stage)
     void* colA;
     void* colB;
+    // TMA staging of the stream's levels (the stage kernels): its kFullMaps maps in device memory (layout of
+    // full_level_maps: tc, guide[0], guide[1], then level L's records at 2 + L), bit L of tma_mask set when
+    // level L's maps were encoded, guide_k the parity of this step's guide; maps == null stages with plain loads
+    const CUtensorMap* maps;
+    unsigned tma_mask;
+    int guide_k;
 };
 
 constexpr int kStages = 2 + 10;
@@ -223,6 +229,7 @@ template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level(const char* __restrict__ table, int cap, int L)
 {
     __shared__ LevelSmem<R> sm;
+    __shared__ __align__(8) uint64_t bar;
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
     const int item = blockIdx.x;
@@ -239,7 +246,15 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level
     lv.last = L == hd->levels - 1;
     lv.lin = res_layout(a.w, a.h, L);
     lv.lout = res_layout(a.w, a.h, L + 1);
-    full_level_tile<ST, R, VAR, PL>(a, lv, level_geom(a.w, a.h, 1 << L, R), item - pf[j], sm);
+    const LevelGeom g = level_geom(a.w, a.h, 1 << L, R);
+    if (e.maps && ((e.tma_mask >> L) & 1u)) {
+        // level 0 stages from the tc plane and this step's guide plane, the others from their records
+        const CUtensorMap* tm = PL ? e.maps : e.maps + 2 + L;
+        const CUtensorMap* tm2 = e.maps + 1 + e.guide_k;
+        full_level_tile_tma<ST, R, VAR, PL, true>(a, lv, g, item - pf[j], sm, bar, tm, tm2);
+    } else {
+        full_level_tile<ST, R, VAR, PL>(a, lv, g, item - pf[j], sm);
+    }
 }
 
 } // namespace tg

@@ -6,6 +6,8 @@
 #include <cstdint>
 #include <string>
 
+#include <cuda.h>
+
 #include "tg_svgf.h"
 
 struct tg_svgf;
@@ -40,5 +42,13 @@ size_t col_var_offset_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 size_t col_guide_half_of(const tg_svgf_params& p, uint32_t w, uint32_t h);
 // Bytes of the per-pixel-block fallback flags of a FULL frame.
 size_t fb_flags_bytes_of(uint32_t w, uint32_t h);
+
+// TMA maps of one FULL stream's a-trous levels for tiles of R output rows per
+// thread: [0] the tc plane, [1] and [2] the guide planes of parity 0 and 1
+// (level 0 stages from these), [2 + L] the input records of level L >= 1.
+// Returns a mask: bit 0 = the three plane maps were encoded, bit L = level L's.
+constexpr int kFullMaps = 12;
+unsigned full_level_maps(const tg_svgf_params& p, uint32_t w, uint32_t h, int R, void* colA, void* colB, void* tc,
+                         void* guide0, void* guide1, CUtensorMap* maps);
 
 } // namespace tg
