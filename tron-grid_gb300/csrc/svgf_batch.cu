@@ -65,9 +65,10 @@ struct tg_svgf_batch {
     int strategy = TG_SVGF_BATCH_STAGES;
     std::vector<int> grids[2];  // per-stage grid of the step in table buffer k
     std::vector<int> sig[2];    // grids the graph of buffer k was captured with
-    // TMA maps of every stream's levels for tiles of 1 and of 2 rows per thread (kFullMaps per stream, built
-    // once: the streams' buffers never move), and which levels of each stream have them
-    CUtensorMap* d_maps[2] = {nullptr, nullptr};
+    // TMA staging of the stage kernels, for tiles of 1 and of 2 rows per thread: each stage's maps of the
+    // first kTmaStreams streams (built once: the streams' buffers never move) and which levels of each stream
+    // have them; empty when no map could be encoded (plain loads)
+    std::vector<StageMaps> stage_maps[2];
     std::vector<unsigned> tma_mask[2];
 };
 
@@ -131,6 +132,7 @@ int set_config(tg_svgf_batch* b, int strategy, int R, int ctas)
 
 using PixFn = void (*)(const char*, int);
 using LevFn = void (*)(const char*, int, int);
+using LevTmaFn = void (*)(const char*, int, int, const StageMaps);
 
 PixFn pixel_kernel(bool f16, int stage)
 {
@@ -151,6 +153,18 @@ LevFn level_kernel(bool f16, int R, int L, int levels)
     return R == 1 ? level_kernel_r<ST_FP32, 1>(L, levels) : level_kernel_r<ST_FP32, 2>(L, levels);
 }
 
+template <int ST, int R> LevTmaFn level_tma_kernel_r(int L, int levels)
+{
+    if (L == 0) return k_ms_level_tma<ST, R, true, true>;
+    return L == levels - 1 ? k_ms_level_tma<ST, R, false, false> : k_ms_level_tma<ST, R, true, false>;
+}
+
+LevTmaFn level_tma_kernel(bool f16, int R, int L, int levels)
+{
+    if (f16) return R == 1 ? level_tma_kernel_r<ST_FP16, 1>(L, levels) : level_tma_kernel_r<ST_FP16, 2>(L, levels);
+    return R == 1 ? level_tma_kernel_r<ST_FP32, 1>(L, levels) : level_tma_kernel_r<ST_FP32, 2>(L, levels);
+}
+
 // One launch per stage over the work table of buffer k.
 cudaError_t launch_stages(tg_svgf_batch* b, int k, cudaStream_t s)
 {
@@ -163,6 +177,9 @@ cudaError_t launch_stages(tg_svgf_batch* b, int k, cudaStream_t s)
         if (g[st] <= 0) continue;
         if (st < 2)
             pixel_kernel(f16, int(st))<<<g[st], dim3(kBlockX, kBlockY), 0, s>>>(b->d_table[k], b->cap);
+        else if (!b->stage_maps[b->R == 1 ? 0 : 1].empty())
+            level_tma_kernel(f16, b->R, int(st) - 2, b->p.levels)<<<g[st], dim3(kLvTX, kLvRows), 0, s>>>(
+                b->d_table[k], b->cap, int(st) - 2, b->stage_maps[b->R == 1 ? 0 : 1][st - 2]);
         else
             level_kernel(f16, b->R, int(st) - 2, b->p.levels)<<<g[st], dim3(kLvTX, kLvRows), 0, s>>>(b->d_table[k], b->cap,
                                                                                                     int(st) - 2);
@@ -304,11 +321,9 @@ void fill_table(tg_svgf_batch* b, int k, uint32_t n, const uint32_t* ids, const 
         ent[j].colA = s.colA;
         ent[j].colB = s.colB;
         const int r = b->R == 1 ? 0 : 1;
-        if (b->d_maps[r]) {
-            ent[j].maps = b->d_maps[r] + size_t(kFullMaps) * ids[j];
-            ent[j].tma_mask = b->tma_mask[r][ids[j]];
-            ent[j].guide_k = cur;
-        }
+        ent[j].tma_slot = (!b->stage_maps[r].empty() && ids[j] < uint32_t(kTmaStreams)) ? int(ids[j]) : -1;
+        ent[j].tma_mask = ent[j].tma_slot >= 0 ? b->tma_mask[r][ids[j]] : 0u;
+        ent[j].guide_k = cur;
         s.frames++;
     }
 }
@@ -360,33 +375,36 @@ void free_batch(tg_svgf_batch* b)
     if (b->h_err) cudaFreeHost(b->h_err);
     if (b->d_bar) cudaFree(b->d_bar);
     if (b->arena) cudaFree(b->arena);
-    for (auto& m : b->d_maps)
-        if (m) cudaFree(m);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
 }
 
-// Encodes every stream's level maps for 1 and 2 rows per thread and copies them to the device; a batch whose
-// maps cannot be built (no encoder, no memory) stages every level with plain loads.
+// Encodes the level maps of the first kTmaStreams streams for 1 and 2 rows per
+// thread and arranges them per stage (StageMaps); a batch whose streams have no
+// encodable map keeps plain loads.
 void build_batch_maps(tg_svgf_batch* b)
 {
-    std::vector<CUtensorMap> h(size_t(kFullMaps) * b->n);
+    CUtensorMap m[kFullMaps];
+    const int nt = b->n < kTmaStreams ? b->n : kTmaStreams;
     for (int r = 0; r < 2; ++r) {
         b->tma_mask[r].assign(b->n, 0u);
+        b->stage_maps[r].assign(b->p.levels, StageMaps{});
         unsigned any = 0;
-        for (int j = 0; j < b->n; ++j) {
+        for (int j = 0; j < nt; ++j) {
             const tg_svgf_batch::Stream& s = b->st[j];
-            b->tma_mask[r][j] = full_level_maps(b->p, b->w[j], b->h[j], r + 1, s.colA, s.colB, s.tc, s.guide[0],
-                                                s.guide[1], &h[size_t(kFullMaps) * j]);
-            any |= b->tma_mask[r][j];
+            const unsigned mask = full_level_maps(b->p, b->w[j], b->h[j], r + 1, s.colA, s.colB, s.tc, s.guide[0],
+                                                  s.guide[1], m);
+            b->tma_mask[r][j] = mask;
+            any |= mask;
+            for (int L = 0; L < b->p.levels; ++L) {
+                if (!((mask >> L) & 1u)) continue;
+                if (L == 0) {
+                    for (int q = 0; q < 3; ++q) b->stage_maps[r][0].m[3 * j + q] = m[q];
+                } else {
+                    b->stage_maps[r][L].m[j] = m[2 + L];
+                }
+            }
         }
-        if (!any) continue;
-        const size_t bytes = h.size() * sizeof(CUtensorMap);
-        if (cudaMalloc(&b->d_maps[r], bytes) != cudaSuccess ||
-            cudaMemcpy(b->d_maps[r], h.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
-            cudaGetLastError();
-            if (b->d_maps[r]) cudaFree(b->d_maps[r]);
-            b->d_maps[r] = nullptr;
-        }
+        if (!any) b->stage_maps[r].clear();
     }
 }
 

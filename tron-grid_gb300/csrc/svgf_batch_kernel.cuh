@@ -37,13 +37,26 @@ struct BatchEntry {
     FullArgs fa;  // stream-level arguments (col_dst = colA for the variance stage)
     void* colA;
     void* colB;
-    // TMA staging of the stream's levels (the stage kernels): its kFullMaps maps in device memory (layout of
-    // full_level_maps: tc, guide[0], guide[1], then level L's records at 2 + L), bit L of tma_mask set when
-    // level L's maps were encoded, guide_k the parity of this step's guide; maps == null stages with plain loads
-    const CUtensorMap* maps;
+    // TMA staging of the stream's levels in the batch's stage kernels (k_ms_level_tma): its slot in the
+    // launch's StageMaps (-1: plain loads), bit L of tma_mask set when level L's maps were encoded, guide_k
+    // the parity of this step's guide
+    int tma_slot;
     unsigned tma_mask;
     int guide_k;
+    int pad;
 };
+
+// Tensor maps of one a-trous stage for the streams of a batch, passed as a
+// kernel parameter (so that, like the single-stream kernels' maps, they need no
+// proxy fence and cannot go stale): level 0 holds each stream's tc, guide[0]
+// and guide[1] plane maps at 3 slot .. 3 slot + 2, level L >= 1 its records' map
+// at slot.  The slot is the stream's id, so the maps do not depend on which
+// streams a step runs, and a captured graph stays valid for any subset.
+constexpr int kTmaStreams = 80;
+struct StageMaps {
+    CUtensorMap m[3 * kTmaStreams];
+};
+static_assert(sizeof(StageMaps) + 64 <= 32764, "stage maps must fit the kernel parameter space");
 
 constexpr int kStages = 2 + 10;
 constexpr long long kBarrierSpinCycles = 2000000000LL;  // default limit, ~1 s at 2 GHz
@@ -229,6 +242,33 @@ template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level(const char* __restrict__ table, int cap, int L)
 {
     __shared__ LevelSmem<R> sm;
+    const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
+    const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
+    const int item = blockIdx.x;
+    if (item >= pf[hd->n]) return;
+    const int j = find_stream(pf, hd->n, item);
+    const BatchEntry& e = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap))[j];
+    const FullArgs& a = e.fa;
+    LevelArgs lv;
+    lv.col_src = (L & 1) ? e.colB : e.colA;
+    lv.col_dst = (L & 1) ? e.colA : e.colB;
+    lv.var_off = a.var_off;
+    lv.ghalf = a.ghalf;
+    lv.level = L;
+    lv.last = L == hd->levels - 1;
+    lv.lin = res_layout(a.w, a.h, L);
+    lv.lout = res_layout(a.w, a.h, L + 1);
+    full_level_tile<ST, R, VAR, PL>(a, lv, level_geom(a.w, a.h, 1 << L, R), item - pf[j], sm);
+}
+
+// The same stage with each stream's tiles staged by TMA through `maps` where
+// its maps exist (tma_slot >= 0 and bit L of tma_mask), with plain loads
+// otherwise.
+template <int ST, int R, bool VAR, bool PL>
+__global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
+    k_ms_level_tma(const char* __restrict__ table, int cap, int L, const __grid_constant__ StageMaps maps)
+{
+    __shared__ LevelSmem<R> sm;
     __shared__ __align__(8) uint64_t bar;
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
@@ -247,11 +287,11 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level
     lv.lin = res_layout(a.w, a.h, L);
     lv.lout = res_layout(a.w, a.h, L + 1);
     const LevelGeom g = level_geom(a.w, a.h, 1 << L, R);
-    if (e.maps && ((e.tma_mask >> L) & 1u)) {
+    if (e.tma_slot >= 0 && ((e.tma_mask >> L) & 1u)) {
         // level 0 stages from the tc plane and this step's guide plane, the others from their records
-        const CUtensorMap* tm = PL ? e.maps : e.maps + 2 + L;
-        const CUtensorMap* tm2 = e.maps + 1 + e.guide_k;
-        full_level_tile_tma<ST, R, VAR, PL, true>(a, lv, g, item - pf[j], sm, bar, tm, tm2);
+        const CUtensorMap* tm = PL ? &maps.m[3 * e.tma_slot] : &maps.m[e.tma_slot];
+        const CUtensorMap* tm2 = PL ? &maps.m[3 * e.tma_slot + 1 + e.guide_k] : tm;
+        full_level_tile_tma<ST, R, VAR, PL>(a, lv, g, item - pf[j], sm, bar, tm, tm2);
     } else {
         full_level_tile<ST, R, VAR, PL>(a, lv, g, item - pf[j], sm);
     }

@@ -556,11 +556,9 @@ __device__ __forceinline__ void tma_tile_body(const FullArgs& a, const LevelArgs
 // records, tc through `tm` and guide_cur through `tm2`, and each staged cell's
 // variance comes from the variance plane, loaded before the wait.  Other levels
 // read `tm` only.
-// One tile `bid` of a level staged by TMA through maps `tm` / `tm2`.  GMAP:
-// the maps live in global memory (written by the host before the launch), so
-// the issuing thread first orders them for the tensor-map proxy; kernel
-// parameter maps need no fence.
-template <int ST, int R, bool VAR, bool PL, bool GMAP>
+// One tile `bid` of a level staged by TMA through maps `tm` / `tm2` (kernel
+// parameters).
+template <int ST, int R, bool VAR, bool PL>
 __device__ __forceinline__ void full_level_tile_tma(const FullArgs& a, const LevelArgs& lv, const LevelGeom& g, int bid,
                                                     LevelSmem<R>& sm, uint64_t& bar, const CUtensorMap* tm,
                                                     const CUtensorMap* tm2)
@@ -576,13 +574,7 @@ __device__ __forceinline__ void full_level_tile_tma(const FullArgs& a, const Lev
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0) {
-        if constexpr (GMAP) {
-            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm) : "memory");
-            if (PL) asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm2) : "memory");
-        }
-        tma_issue<ST, R, PL>(g, ra, rb, i0, j0, sm, ubar, tm, tm2);
-    }
+    if (tid == 0) tma_issue<ST, R, PL>(g, ra, rb, i0, j0, sm, ubar, tm, tm2);
     if (tile_interior<R>(a, g.s, ra, rb, i0, j0))
         tma_tile_body<ST, R, VAR, PL, true>(a, lv, g, ra, rb, i0, j0, tid, ubar, sm);
     else
@@ -596,7 +588,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
 {
     __shared__ LevelSmem<R> sm;
     __shared__ __align__(8) uint64_t bar;
-    full_level_tile_tma<ST, R, VAR, PL, false>(a, lv, g, blockIdx.x, sm, bar, &tm, &tm2);
+    full_level_tile_tma<ST, R, VAR, PL>(a, lv, g, blockIdx.x, sm, bar, &tm, &tm2);
 }
 
 // ------------------------------------------------------------- REF-EXACT ----
