@@ -127,6 +127,10 @@ struct Sess {
     tg_image in_view[4];  // the current frame's inputs as the kernels read them (a slot, or mapped host memory)
     char* out_slot[2];
     uint64_t frames = 0, lru = 0;
+    // TMA maps of the session's a-trous levels (full_level_maps layout), encoded at admission, and which levels
+    // have them
+    CUtensorMap maps[kFullMaps];
+    unsigned tma_mask = 0;
     int pending = 0;  // queued + running frames
     int running = 0;  // frames in launches not yet complete (at most 2)
 };
@@ -172,6 +176,7 @@ struct tg_svgf_server {
     BarrierState* d_bar = nullptr;
     cudaGraphExec_t exec[kMaxInflight] = {};
     std::vector<cudaEvent_t> ev_pool;  // completion events, reused
+    StageMaps stage_maps[10];          // the stage kernels' maps of the launch being formed (one per level)
     bool graphs_ok = true;
     // stats
     uint64_t submitted = 0, completed = 0, failed = 0, admissions = 0, evictions = 0, n_launches = 0;
@@ -239,6 +244,7 @@ void carve(tg_svgf_server* sv, Sess& s)
         s.out_slot[f] = p;
         p += al256(size_t(fmt_bytes(s.fmt[4])) * np);
     }
+    s.tma_mask = full_level_maps(sv->d.params, s.w, s.h, kR, s.colA, s.colB, s.tc, s.guide[0], s.guide[1], s.maps);
 }
 
 void release(tg_svgf_server* sv, Sess& s)
@@ -356,11 +362,12 @@ void launch_stage_kernels(tg_svgf_server* sv, int k, const std::vector<int>& gri
             // level 0 stages from the planes, the last level writes only colour
             const int L = int(g) - 2;
             const bool pl = L == 0, var = pl || L != sv->d.params.levels - 1;
-            auto k16 = pl ? k_ms_level<ST_FP16, kR, true, true>
-                          : (var ? k_ms_level<ST_FP16, kR, true, false> : k_ms_level<ST_FP16, kR, false, false>);
-            auto k32 = pl ? k_ms_level<ST_FP32, kR, true, true>
-                          : (var ? k_ms_level<ST_FP32, kR, true, false> : k_ms_level<ST_FP32, kR, false, false>);
-            (sv->f16 ? k16 : k32)<<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, L);
+            auto k16 = pl ? k_ms_level_tma<ST_FP16, kR, true, true>
+                          : (var ? k_ms_level_tma<ST_FP16, kR, true, false> : k_ms_level_tma<ST_FP16, kR, false, false>);
+            auto k32 = pl ? k_ms_level_tma<ST_FP32, kR, true, true>
+                          : (var ? k_ms_level_tma<ST_FP32, kR, true, false> : k_ms_level_tma<ST_FP32, kR, false, false>);
+            (sv->f16 ? k16 : k32)<<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, L,
+                                                                               sv->stage_maps[L]);
         }
     }
 }
@@ -391,10 +398,26 @@ void launch_batch(tg_svgf_server* sv, std::vector<Sess*>& ss, int k)
         pf[n] = acc;
         grids[stage] = stage == 1 ? variance_grid(acc, sv->sm_count) : acc;
     }
+    // the stage kernels' maps: slot j of each stage's StageMaps holds the j-th frame's session's maps
+    const bool stages = sv->d.strategy == TG_SVGF_BATCH_STAGES;
     for (int j = 0; j < n; ++j) {
-        ent[j].fa = args_for(sv, *ss[j]);
-        ent[j].colA = ss[j]->colA;
-        ent[j].colB = ss[j]->colB;
+        Sess& sj = *ss[j];
+        ent[j].fa = args_for(sv, sj);
+        ent[j].colA = sj.colA;
+        ent[j].colB = sj.colB;
+        ent[j].tma_slot = -1;
+        if (stages && j < kTmaStreams && sj.tma_mask) {
+            ent[j].tma_slot = j;
+            ent[j].tma_mask = sj.tma_mask;
+            ent[j].guide_k = int(sj.frames & 1u);
+            for (int L = 0; L < hd->levels; ++L) {
+                if (!((sj.tma_mask >> L) & 1u)) continue;
+                if (L == 0)
+                    for (int q = 0; q < 3; ++q) sv->stage_maps[0].m[3 * j + q] = sj.maps[q];
+                else
+                    sv->stage_maps[L].m[j] = sj.maps[2 + L];
+            }
+        }
     }
     if (sv->d.strategy == TG_SVGF_BATCH_STAGES) {
         launch_stage_kernels(sv, k, grids);
@@ -448,12 +471,26 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
         a.lout = res_layout(a.w, a.h, lv + 1);
         const LevelGeom g = level_geom(a.w, a.h, a.stride, kR);
         const dim3 lgrid(level_blocks(g)), lblk(kLvTX, kLvRows);
-        // level 0 stages from the planes, the last level writes only colour
-        auto k16 = lv == 0 ? k_full_level_tiled<ST_FP16, kR, true, true>
-                           : (a.last ? k_full_level_tiled<ST_FP16, kR, false> : k_full_level_tiled<ST_FP16, kR, true>);
-        auto k32 = lv == 0 ? k_full_level_tiled<ST_FP32, kR, true, true>
-                           : (a.last ? k_full_level_tiled<ST_FP32, kR, false> : k_full_level_tiled<ST_FP32, kR, true>);
-        (sv->f16 ? k16 : k32)<<<lgrid, lblk, 0, st>>>(a, g);
+        // level 0 stages from the planes, the last level writes only colour; tiles are staged by TMA where the
+        // session's maps were encoded, as the single-stream path does
+        if ((s.tma_mask >> lv) & 1u) {
+            const LevelArgs la = level_args_of(a);
+            const CUtensorMap& tm = lv == 0 ? s.maps[0] : s.maps[2 + lv];
+            const CUtensorMap& tm2 = lv == 0 ? s.maps[1 + int(s.frames & 1u)] : tm;
+            auto t16 = lv == 0 ? k_full_level_tma<ST_FP16, kR, true, true>
+                               : (a.last ? k_full_level_tma<ST_FP16, kR, false, false>
+                                         : k_full_level_tma<ST_FP16, kR, true, false>);
+            auto t32 = lv == 0 ? k_full_level_tma<ST_FP32, kR, true, true>
+                               : (a.last ? k_full_level_tma<ST_FP32, kR, false, false>
+                                         : k_full_level_tma<ST_FP32, kR, true, false>);
+            (sv->f16 ? t16 : t32)<<<lgrid, lblk, 0, st>>>(a, la, g, tm, tm2);
+        } else {
+            auto k16 = lv == 0 ? k_full_level_tiled<ST_FP16, kR, true, true>
+                               : (a.last ? k_full_level_tiled<ST_FP16, kR, false> : k_full_level_tiled<ST_FP16, kR, true>);
+            auto k32 = lv == 0 ? k_full_level_tiled<ST_FP32, kR, true, true>
+                               : (a.last ? k_full_level_tiled<ST_FP32, kR, false> : k_full_level_tiled<ST_FP32, kR, true>);
+            (sv->f16 ? k16 : k32)<<<lgrid, lblk, 0, st>>>(a, g);
+        }
         std::swap(src, oth);
     }
 }
