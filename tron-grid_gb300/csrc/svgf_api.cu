@@ -672,18 +672,12 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
         // temporal: inputs + previous guide/history/moments, writes guide, tc, moments, depth gradient and
         // the variance plane entry (every pixel with a history of fallback_frames or more)
         launch(s, stream, F_FULL_TEMPORAL, npx * (inb + 2 * (gb + c4 + mm) + 8 + vb), [&] {
-            if (f16)
-                k_full_temporal<ST_FP16><<<grd, blk, 0, stream>>>(a);
-            else
-                k_full_temporal<ST_FP32><<<grd, blk, 0, stream>>>(a);
+            launch_chain(f16 ? k_full_temporal<ST_FP16> : k_full_temporal<ST_FP32>, grd, blk, stream, a);
         });
         // variance: the block flags; the flagged blocks' short-history pixels (data-dependent, not counted)
         launch(s, stream, F_FULL_VARIANCE, double(fb_flags_bytes_of(s->w, s->h)), [&] {
             const int vg = variance_grid(int(grd.x * grd.y), s->sms);
-            if (f16)
-                k_full_variance<ST_FP16><<<vg, blk, 0, stream>>>(a);
-            else
-                k_full_variance<ST_FP32><<<vg, blk, 0, stream>>>(a);
+            launch_chain(f16 ? k_full_variance<ST_FP16> : k_full_variance<ST_FP32>, dim3(vg), blk, stream, a);
         });
         void* src = s->colA;
         void* oth = s->colB;
@@ -707,11 +701,14 @@ int launch_frame(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outputs* ou
                 if (s->tma && (!pl || s->tma0)) {
                     const LevelArgs la = level_args_of(a);
                     if (pl)
-                        level_tma_kernel<true>(f16, a.last)<<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tm_tc, s->tm_guide[cur]);
+                        launch_chain(level_tma_kernel<true>(f16, a.last), lgrid, lblk, stream, a, la, lg, s->tm_tc,
+                                     s->tm_guide[cur]);
                     else
-                        level_tma_kernel<false>(f16, a.last)<<<lgrid, lblk, 0, stream>>>(a, la, lg, s->tmaps[lv], s->tmaps[lv]);
+                        launch_chain(level_tma_kernel<false>(f16, a.last), lgrid, lblk, stream, a, la, lg, s->tmaps[lv],
+                                     s->tmaps[lv]);
                 } else {
-                    (pl ? level_tiled_kernel<true>(f16, a.last) : level_tiled_kernel<false>(f16, a.last))<<<lgrid, lblk, 0, stream>>>(a, lg);
+                    launch_chain(pl ? level_tiled_kernel<true>(f16, a.last) : level_tiled_kernel<false>(f16, a.last), lgrid,
+                                 lblk, stream, a, lg);
                 }
             });
             void* t = src;

@@ -8,11 +8,49 @@
 #pragma once
 
 #include <cuda_fp16.h>
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "tg_svgf.h"
 
+// Chain kernels are launched with programmatic stream serialization (PDL) when
+// this is 1: a kernel's CTAs are scheduled while the previous kernel of the
+// stream drains, and wait in pdl_begin() for its completion.
+#ifndef TG_PDL
+#define TG_PDL 1
+#endif
+
 namespace tg {
+
+// First statement of every chain kernel.  griddepcontrol.wait holds the CTA
+// until the previous kernel of the stream has completed and its writes are
+// visible (it returns at once for a kernel launched without programmatic
+// serialization); launch_dependents then allows the next kernel's CTAs to be
+// scheduled once every CTA of this grid has started, so they never take an SM
+// slot from a CTA of this grid that has not.
+__device__ __forceinline__ void pdl_begin()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches a chain kernel on `st`, with programmatic stream serialization when
+// TG_PDL is set (the kernel must begin with pdl_begin()).
+template <class... P, class... A>
+inline cudaError_t launch_chain(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = TG_PDL ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<A&&>(args)...);
+}
 
 enum Storage : int { ST_FP32 = 0, ST_FP16 = 1 };
 

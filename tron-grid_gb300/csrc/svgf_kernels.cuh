@@ -366,6 +366,7 @@ __device__ __forceinline__ void variance_compact(int base, int stride, int items
 
 template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY, 4) k_full_temporal(FullArgs a)
 {
+    pdl_begin();
     full_temporal_block<ST>(a, blockIdx.y * gridDim.x + blockIdx.x, blockIdx.x * kBlockX + threadIdx.x,
                             blockIdx.y * kBlockY + threadIdx.y);
 }
@@ -375,6 +376,7 @@ template <int ST> __global__ void __launch_bounds__(kBlockX* kBlockY) k_full_var
 {
     __shared__ VarTile vt;
     __shared__ VarList l;
+    pdl_begin();
     const int tx = (a.w + kBlockX - 1) / kBlockX, items = tx * ((a.h + kBlockY - 1) / kBlockY);
     const int* flags = a.fb_flags;
     variance_compact(int(blockIdx.x), int(gridDim.x), items, [flags](int b) { return __ldcg(flags + b) != 0; }, l);

@@ -387,6 +387,7 @@ template <int ST, int R, bool VAR, bool PL = false>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_level_tiled(FullArgs a, LevelGeom g)
 {
     __shared__ LevelSmem<R> sm;
+    pdl_begin();
     full_level_tile<ST, R, VAR, PL>(a, level_args_of(a), g, blockIdx.x, sm);
 }
 
@@ -588,6 +589,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
 {
     __shared__ LevelSmem<R> sm;
     __shared__ __align__(8) uint64_t bar;
+    pdl_begin();
     full_level_tile_tma<ST, R, VAR, PL>(a, lv, g, blockIdx.x, sm, bar, &tm, &tm2);
 }
 
@@ -820,6 +822,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, TG_REF_FIRST_CTAS)
     __shared__ float4 sA[T::N];
     __shared__ __align__(128) float4 land[T::N];
     __shared__ __align__(8) uint64_t bar;
+    pdl_begin();
     const int i0 = int(blockIdx.x % unsigned(g.tiles_x)) * T::TX;
     const int j0 = int(blockIdx.x / unsigned(g.tiles_x)) * T::TY;
     const bool in = ref_tile_interior<R>(a.w, a.h, 1, 0, 0, i0, j0);
@@ -904,6 +907,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, TG_REF_CTAS)
     __shared__ float4 sA[T::N];
     __shared__ __align__(128) float4 land[T::N];
     __shared__ __align__(8) uint64_t bar;
+    pdl_begin();
     int ra, rb, i0, j0;
     level_block(g, blockIdx.x, T::TX, T::TY, ra, rb, i0, j0);
     const bool in = ref_tile_interior<R>(a.w, a.h, g.s, ra, rb, i0, j0);
@@ -971,10 +975,8 @@ void enqueue_ref_chain(RefArgs a, void* wa, void* wb, int levels, bool f16, cuda
     hook(true, [&] {
         const CUtensorMap& m = maps.first ? *maps.first : none;
         const int t = maps.first != nullptr;
-        if (f16)
-            k_ref_first<ST_FP16, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0, m, t);
-        else
-            k_ref_first<ST_FP32, R><<<level_blocks(g0), blk, 0, stream>>>(a, g0, m, t);
+        launch_chain(f16 ? k_ref_first<ST_FP16, R> : k_ref_first<ST_FP32, R>, dim3(level_blocks(g0)), blk, stream, a, g0,
+                     m, t);
     });
     void* src = wb;
     void* oth = wa;
@@ -989,10 +991,8 @@ void enqueue_ref_chain(RefArgs a, void* wa, void* wb, int levels, bool f16, cuda
         hook(false, [&] {
             const CUtensorMap& m = maps.level[lv] ? *maps.level[lv] : none;
             const int t = maps.level[lv] != nullptr;
-            if (f16)
-                k_ref_level<ST_FP16, R><<<level_blocks(g), blk, 0, stream>>>(a, g, m, t);
-            else
-                k_ref_level<ST_FP32, R><<<level_blocks(g), blk, 0, stream>>>(a, g, m, t);
+            launch_chain(f16 ? k_ref_level<ST_FP16, R> : k_ref_level<ST_FP32, R>, dim3(level_blocks(g)), blk, stream, a,
+                         g, m, t);
         });
         void* t = src;
         src = oth;
