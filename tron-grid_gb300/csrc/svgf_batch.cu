@@ -175,15 +175,16 @@ cudaError_t launch_stages(tg_svgf_batch* b, int k, cudaStream_t s)
     const std::vector<int>& g = b->grids[k];
     for (size_t st = 0; st < g.size(); ++st) {
         if (g[st] <= 0) continue;
+        const char* tab = b->d_table[k];
+        const int L = int(st) - 2;
         if (st < 2)
-            pixel_kernel(f16, int(st))<<<g[st], dim3(kBlockX, kBlockY), 0, s>>>(b->d_table[k], b->cap);
+            e = launch_chain(pixel_kernel(f16, int(st)), dim3(g[st]), dim3(kBlockX, kBlockY), s, tab, b->cap);
         else if (!b->stage_maps[b->R == 1 ? 0 : 1].empty())
-            level_tma_kernel(f16, b->R, int(st) - 2, b->p.levels)<<<g[st], dim3(kLvTX, kLvRows), 0, s>>>(
-                b->d_table[k], b->cap, int(st) - 2, b->stage_maps[b->R == 1 ? 0 : 1][st - 2]);
+            e = launch_chain(level_tma_kernel(f16, b->R, L, b->p.levels), dim3(g[st]), dim3(kLvTX, kLvRows), s, tab, b->cap,
+                             L, b->stage_maps[b->R == 1 ? 0 : 1][st - 2]);
         else
-            level_kernel(f16, b->R, int(st) - 2, b->p.levels)<<<g[st], dim3(kLvTX, kLvRows), 0, s>>>(b->d_table[k], b->cap,
-                                                                                                    int(st) - 2);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            e = launch_chain(level_kernel(f16, b->R, L, b->p.levels), dim3(g[st]), dim3(kLvTX, kLvRows), s, tab, b->cap, L);
+        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }

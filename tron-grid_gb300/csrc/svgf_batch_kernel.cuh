@@ -204,6 +204,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __
 template <int ST, int STAGE>
 __global__ void __launch_bounds__(kBlockX* kBlockY) k_ms_pixel(const char* __restrict__ table, int cap)
 {
+    pdl_begin();
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + STAGE * (cap + 1);
     const BatchEntry* ent = reinterpret_cast<const BatchEntry*>(table + table_entries_offset(cap));
@@ -242,6 +243,7 @@ template <int ST, int R, bool VAR, bool PL>
 __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_ms_level(const char* __restrict__ table, int cap, int L)
 {
     __shared__ LevelSmem<R> sm;
+    pdl_begin();
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
     const int item = blockIdx.x;
@@ -270,6 +272,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas)
 {
     __shared__ LevelSmem<R> sm;
     __shared__ __align__(8) uint64_t bar;
+    pdl_begin();
     const BatchHeader* hd = reinterpret_cast<const BatchHeader*>(table);
     const int* pf = reinterpret_cast<const int*>(table + table_prefix_offset()) + (2 + L) * (cap + 1);
     const int item = blockIdx.x;

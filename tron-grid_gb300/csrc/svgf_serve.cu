@@ -351,13 +351,11 @@ void launch_stage_kernels(tg_svgf_server* sv, int k, const std::vector<int>& gri
     cudaMemcpyAsync(sv->d_table[k], sv->h_table[k], sv->tbytes, cudaMemcpyHostToDevice, st);
     for (size_t g = 0; g < grids.size(); ++g) {
         if (grids[g] <= 0) continue;
+        const char* tab = sv->d_table[k];
         if (g < 2) {
-            if (sv->f16)
-                (g == 0 ? k_ms_pixel<ST_FP16, 0> : k_ms_pixel<ST_FP16, 1>)<<<grids[g], dim3(kBlockX, kBlockY), 0, st>>>(
-                    sv->d_table[k], sv->cap);
-            else
-                (g == 0 ? k_ms_pixel<ST_FP32, 0> : k_ms_pixel<ST_FP32, 1>)<<<grids[g], dim3(kBlockX, kBlockY), 0, st>>>(
-                    sv->d_table[k], sv->cap);
+            auto p16 = g == 0 ? k_ms_pixel<ST_FP16, 0> : k_ms_pixel<ST_FP16, 1>;
+            auto p32 = g == 0 ? k_ms_pixel<ST_FP32, 0> : k_ms_pixel<ST_FP32, 1>;
+            launch_chain(sv->f16 ? p16 : p32, dim3(grids[g]), dim3(kBlockX, kBlockY), st, tab, sv->cap);
         } else {
             // level 0 stages from the planes, the last level writes only colour
             const int L = int(g) - 2;
@@ -366,8 +364,7 @@ void launch_stage_kernels(tg_svgf_server* sv, int k, const std::vector<int>& gri
                           : (var ? k_ms_level_tma<ST_FP16, kR, true, false> : k_ms_level_tma<ST_FP16, kR, false, false>);
             auto k32 = pl ? k_ms_level_tma<ST_FP32, kR, true, true>
                           : (var ? k_ms_level_tma<ST_FP32, kR, true, false> : k_ms_level_tma<ST_FP32, kR, false, false>);
-            (sv->f16 ? k16 : k32)<<<grids[g], dim3(kLvTX, kLvRows), 0, st>>>(sv->d_table[k], sv->cap, L,
-                                                                               sv->stage_maps[L]);
+            launch_chain(sv->f16 ? k16 : k32, dim3(grids[g]), dim3(kLvTX, kLvRows), st, tab, sv->cap, L, sv->stage_maps[L]);
         }
     }
 }
@@ -452,13 +449,8 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
     const dim3 grd((s.w + kBlockX - 1) / kBlockX, (s.h + kBlockY - 1) / kBlockY);
     cudaStream_t st = sv->s_comp;
     const int vg = variance_grid(int(grd.x * grd.y), sv->sm_count);
-    if (sv->f16) {
-        k_full_temporal<ST_FP16><<<grd, blk, 0, st>>>(a);
-        k_full_variance<ST_FP16><<<vg, blk, 0, st>>>(a);
-    } else {
-        k_full_temporal<ST_FP32><<<grd, blk, 0, st>>>(a);
-        k_full_variance<ST_FP32><<<vg, blk, 0, st>>>(a);
-    }
+    launch_chain(sv->f16 ? k_full_temporal<ST_FP16> : k_full_temporal<ST_FP32>, grd, blk, st, a);
+    launch_chain(sv->f16 ? k_full_variance<ST_FP16> : k_full_variance<ST_FP32>, dim3(vg), blk, st, a);
     void* src = s.colA;
     void* oth = s.colB;
     for (int lv = 0; lv < sv->d.params.levels; ++lv) {
@@ -483,13 +475,13 @@ void launch_plain(tg_svgf_server* sv, Sess& s)
             auto t32 = lv == 0 ? k_full_level_tma<ST_FP32, kR, true, true>
                                : (a.last ? k_full_level_tma<ST_FP32, kR, false, false>
                                          : k_full_level_tma<ST_FP32, kR, true, false>);
-            (sv->f16 ? t16 : t32)<<<lgrid, lblk, 0, st>>>(a, la, g, tm, tm2);
+            launch_chain(sv->f16 ? t16 : t32, lgrid, lblk, st, a, la, g, tm, tm2);
         } else {
             auto k16 = lv == 0 ? k_full_level_tiled<ST_FP16, kR, true, true>
                                : (a.last ? k_full_level_tiled<ST_FP16, kR, false> : k_full_level_tiled<ST_FP16, kR, true>);
             auto k32 = lv == 0 ? k_full_level_tiled<ST_FP32, kR, true, true>
                                : (a.last ? k_full_level_tiled<ST_FP32, kR, false> : k_full_level_tiled<ST_FP32, kR, true>);
-            (sv->f16 ? k16 : k32)<<<lgrid, lblk, 0, st>>>(a, g);
+            launch_chain(sv->f16 ? k16 : k32, lgrid, lblk, st, a, g);
         }
         std::swap(src, oth);
     }
