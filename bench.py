@@ -967,10 +967,40 @@ def run_e2e(args, frames, dev, mode, storage, world, t0=0):
     el = max_over_ranks(c1 - c0, world, dev)
     total = sum_over_ranks(float(steps), world, dev)
     den.close()
+    link_ms = link_ms_per_step(host, houts, dev, steps)
     return {"value": total / el, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": el / steps * 1e3, "host_frames_cycled": n_host,
             "frames": f"sequence frames {t0}..{(t0 + n_host - 1) % len(frames)}, cycled",
-            "api": "tg_svgf_denoise_host (pinned host buffers, a ring of three staging sets)"}
+            "api": "tg_svgf_denoise_host (pinned host buffers, a ring of three staging sets)",
+            "copies_only_ms_per_step": link_ms, "link_bound_frames_per_s": 1e3 / link_ms,
+            "frac_of_link_bound": (total / el) / (1e3 / link_ms),
+            "link_bound": "the same copies with no compute: each step's inputs host->device on one stream and an "
+                          "output device->host on another, concurrently (the host link's ceiling for this API)"}
+
+
+def link_ms_per_step(host, houts, dev, steps):
+    """Milliseconds per step of the end-to-end path's copies alone: the step's pinned inputs host->device on one
+    stream while an output goes device->host on a second, as the denoiser's pipeline overlaps them."""
+    import torch
+
+    dbuf = {k: torch.empty(v.shape, dtype=v.dtype, device=dev) for k, v in host[0].items()}
+    dout = torch.empty(houts[0].shape, dtype=houts[0].dtype, device=dev)
+    s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def go(n):
+        for i in range(n):
+            with torch.cuda.stream(s_in):
+                for k, v in host[i % len(host)].items():
+                    dbuf[k].copy_(v, non_blocking=True)
+            with torch.cuda.stream(s_out):
+                houts[i % len(houts)].copy_(dout, non_blocking=True)
+
+    go(3)
+    torch.cuda.synchronize()
+    c0 = time.perf_counter()
+    go(steps)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - c0) / steps * 1e3
 
 
 def run_cpu_baseline(args, spec, seconds=15.0, frames=None, start=0, warm=3):

@@ -146,6 +146,7 @@ struct Flight {
     std::vector<Sess*> sess;
     cudaEvent_t ev_comp = nullptr, ev_d2h = nullptr;
     int table_k = -1;
+    bool launch_failed = false;  // a kernel of this launch was rejected at launch time
 };
 
 } // namespace
@@ -664,6 +665,7 @@ void scheduler(tg_svgf_server* sv)
             launch_batch(sv, ss, k);
         else
             launch_plain(sv, *ss[0]);
+        fl->launch_failed = cudaGetLastError() != cudaSuccess;
         cudaEventRecord(fl->ev_comp, sv->s_comp);
         cudaStreamWaitEvent(sv->s_d2h, fl->ev_comp, 0);
         for (size_t j = 0; j < batch.size(); ++j) {
@@ -707,7 +709,7 @@ void completer(tg_svgf_server* sv)
             fl = sv->inflight.front();
         }
         const cudaError_t e = cudaEventSynchronize(fl->ev_d2h);
-        int status = e == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+        int status = (e == cudaSuccess && !fl->launch_failed) ? TG_OK : TG_ERR_CUDA;
         if (status == TG_OK && fl->table_k >= 0 && sv->h_err[fl->table_k]) {
             sv->h_err[fl->table_k] = 0;
             status = TG_ERR_TIMEOUT;
