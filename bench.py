@@ -193,7 +193,7 @@ def sum_over_ranks(v, world, device):
 def workload(args):
     from tron_grid_gb300 import scene
 
-    spec = scene.config1(args.width, args.height, seed=0)
+    spec = scene.pan_with_disocclusion(args.width, args.height, seed=0)
     name = (f"{'FULL' if args.mode == 'full' else 'REF_EXACT'} SVGF {args.width}x{args.height}, "
             f"{args.storage.upper()} storage, {5 if args.mode == 'full' else 3} a-trous levels, "
             f"{args.pool}-frame synthetic sequence (yaw 0.5 deg + 0.05 m per frame, plane appears at frame 30)")
@@ -384,7 +384,7 @@ def run_single(args, dev, mode_s, storage_s, steps, size=None):
 
     spec, _ = workload(args)
     if size is not None:
-        spec = scene.config1(size[0], size[1], seed=0)
+        spec = scene.pan_with_disocclusion(size[0], size[1], seed=0)
     W, H = spec.width, spec.height
     frames = gen_frames(spec, min(args.pool, 30), dev, storage_s, mode_s)
     mode = tg.MODE_FULL if mode_s == "full" else tg.MODE_REF_EXACT
@@ -522,7 +522,7 @@ def run_post(args, dev, steps=200, cpu=True):
            "algo_bytes_per_px": 12, "l2": "flushed (256 MB write) before every timed frame"}
     hdr4k = None
     for name, (W, H) in (("3840x2160", (3840, 2160)), ("1280x720", (1280, 720))):
-        sc = scene.PlaneScene(scene.config1(W, H, seed=0), device=dev)
+        sc = scene.PlaneScene(scene.pan_with_disocclusion(W, H, seed=0), device=dev)
         pool = [sc.frame(t)["radiance"].to(torch.float16).contiguous() for t in range(4)]
         if hdr4k is None:
             hdr4k = pool[0].float().cpu().numpy()
@@ -636,7 +636,7 @@ def run_eye(args, dev, steps=200, cpu=True):
 
 
 def run_batched(args, dev):
-    """BASELINE config 3: N streams of seeded resolutions, FP16, one persistent launch per step (autotuned,
+    """Many-stream batch: N streams of seeded resolutions, FP16, one persistent launch per step (autotuned,
     graph-replayed), against the plain per-stream FP32 path on the same frames."""
     import numpy as np
     import torch
@@ -729,7 +729,7 @@ def run_batched(args, dev):
 
 
 def run_serving(args, dev):
-    """BASELINE config 4: sessions of seeded resolutions submit frames as a Poisson process (aggregate rate),
+    """Serving: sessions of seeded resolutions submit frames as a Poisson process (aggregate rate),
     each session alternating exponential(2 s) idle and active periods; continuous batching (FP16 storage)
     against plain per-request launches (FP32 storage) on the same arrivals; 24 GB budget."""
     import numpy as np
@@ -877,7 +877,7 @@ def run_accuracy(dev, W=3840, H=2160, frames=60):
     import tron_grid_gb300 as tg
     from tron_grid_gb300 import scene
 
-    sc = scene.PlaneScene(scene.config1(W, H, seed=0), device=dev)
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(W, H, seed=0), device=dev)
     d32 = tg.Denoiser(W, H, storage=tg.STORAGE_FP32, device=dev.index)
     d16 = tg.Denoiser(W, H, storage=tg.STORAGE_FP16, device=dev.index)
     st = oracle.FullState(H, W, np.float64)

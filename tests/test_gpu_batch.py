@@ -20,7 +20,7 @@ SIZES = [(17, 9), (64, 36), (160, 90), (33, 17), (96, 64), (1, 1)]
 
 
 def _streams(sizes, frames, dev, f16=False, seed=0):
-    specs = [scene.config1(w, h, seed=seed + 13 * k) for k, (w, h) in enumerate(sizes)]
+    specs = [scene.pan_with_disocclusion(w, h, seed=seed + 13 * k) for k, (w, h) in enumerate(sizes)]
     out = []
     for sp in specs:
         sc = scene.PlaneScene(sp)

@@ -38,7 +38,7 @@ def _sequence(W, H, order, storage, check, with_f64, dev):
     (float32 with the storage form's rounding; with `with_f64` also float64 on the full-precision inputs and,
     for FP16 storage, float64 on the same binary16 radiance and octahedral normals the GPU gets), calling
     check(t, gpu, r32, r64, r64q) for each frame (r64q is r64 for FP32 storage)."""
-    sc = scene.PlaneScene(scene.config1(W, H, seed=0), device=dev)
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(W, H, seed=0), device=dev)
     f16 = storage == tg.STORAGE_FP16
     den = tg.Denoiser(W, H, mode=tg.MODE_FULL, storage=storage)
     P = oracle.full_params()

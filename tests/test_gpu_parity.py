@@ -77,20 +77,20 @@ def _check_fp32(t, g, r32, r64):
     assert rel_l2(g, r64) <= 1e-4, f"frame {t}: rel L2 vs float64 {rel_l2(g, r64):.3e}"
 
 
-def test_full_fp32_config0(cuda_dev):
+def test_full_fp32_640x360_pan(cuda_dev):
     """640x360, 8 frames, yaw 0.2 deg/frame, 5 levels, sigma 4/128/1."""
-    _run_full_pair(cuda_dev, scene.config0(seed=1), 8, check=_check_fp32)
+    _run_full_pair(cuda_dev, scene.slow_pan(seed=1), 8, check=_check_fp32)
 
 
 def test_full_fp32_motion_and_disocclusion(cuda_dev):
     """Yaw 0.5 deg + 0.05 m per frame with a plane appearing at frame 30 (320x180)."""
-    spec = scene.config1(320, 180, seed=2)
+    spec = scene.pan_with_disocclusion(320, 180, seed=2)
     _run_full_pair(cuda_dev, spec, 33, check=_check_fp32)
 
 
 @pytest.mark.parametrize("wh", [(1, 1), (2, 2), (7, 3), (33, 17), (5, 40)])
 def test_full_fp32_odd_sizes(cuda_dev, wh):
-    spec = scene.config1(wh[0], wh[1], seed=3)
+    spec = scene.pan_with_disocclusion(wh[0], wh[1], seed=3)
     _run_full_pair(cuda_dev, spec, 5, check=_check_fp32)
 
 
@@ -105,7 +105,7 @@ def _check_fp16(t, g, r32, r64):
 
 def test_full_fp16_storage(cuda_dev):
     """FP16 colour/moments, octahedral normals; FP16 radiance + OCT16 normal inputs."""
-    _run_full_pair(cuda_dev, scene.config1(320, 180, seed=4), 33, storage=tg.STORAGE_FP16, fp16_inputs=True,
+    _run_full_pair(cuda_dev, scene.pan_with_disocclusion(320, 180, seed=4), 33, storage=tg.STORAGE_FP16, fp16_inputs=True,
                    check=_check_fp16)
 
 
@@ -117,13 +117,13 @@ ODD_PARAMS = dict(sigma_l=2.5, sigma_n=64.0, sigma_z=0.5, alpha=0.1, moments_alp
 @pytest.mark.parametrize("levels", [1, 2, 3, 4])
 def test_full_fp32_level_counts_and_params(cuda_dev, levels):
     """Fewer a-trous levels (with one level, level 0 is also the last: staged from the planes, colour only)."""
-    _run_full_pair(cuda_dev, scene.config1(96, 64, seed=5), 6, check=_check_fp32, params=dict(ODD_PARAMS, levels=levels))
+    _run_full_pair(cuda_dev, scene.pan_with_disocclusion(96, 64, seed=5), 6, check=_check_fp32, params=dict(ODD_PARAMS, levels=levels))
 
 
 @pytest.mark.parametrize("W", [96, 97])
 def test_full_fp16_single_level(cuda_dev, W):
     """One FP16 level at an even width (level 0 by TMA from the planes) and an odd one (plain loads)."""
-    _run_full_pair(cuda_dev, scene.config1(W, 64, seed=6), 6, storage=tg.STORAGE_FP16, fp16_inputs=True,
+    _run_full_pair(cuda_dev, scene.pan_with_disocclusion(W, 64, seed=6), 6, storage=tg.STORAGE_FP16, fp16_inputs=True,
                    check=_check_fp16, params=dict(ODD_PARAMS, levels=1))
 
 
@@ -150,7 +150,7 @@ def test_ref_exact_fp32(cuda_dev):
         assert e.max() <= REL_TOL, f"frame {t}: {report(g, r)}"
         assert np.all(g[..., 3] == 1.0)
 
-    _ref_pair(cuda_dev, scene.config0(seed=5), 8, tg.STORAGE_FP32, chk)
+    _ref_pair(cuda_dev, scene.slow_pan(seed=5), 8, tg.STORAGE_FP32, chk)
 
 
 def test_ref_exact_fp16_images(cuda_dev):
@@ -163,7 +163,7 @@ def test_ref_exact_fp16_images(cuda_dev):
         same = np.mean(g[..., :3] == r[..., :3])
         assert same >= 0.999, f"frame {t}: only {same:.5f} of values identical"
 
-    _ref_pair(cuda_dev, scene.config0(seed=6), 8, tg.STORAGE_FP16, chk)
+    _ref_pair(cuda_dev, scene.slow_pan(seed=6), 8, tg.STORAGE_FP16, chk)
 
 
 @pytest.mark.parametrize("wh", [(1, 1), (2, 2), (7, 3), (33, 17)])
@@ -178,7 +178,7 @@ def test_ref_exact_odd_sizes(cuda_dev, wh):
 def test_host_api_matches_device_api(cuda_dev, storage):
     """tg_svgf_denoise_host (pinned host buffers, four frames through its ring of three staging sets) gives the
     device API's bits; FP16 storage with rgba16f radiance and octahedral normals."""
-    spec = scene.config1(200, 120, seed=9)
+    spec = scene.pan_with_disocclusion(200, 120, seed=9)
     frames = _frames(spec, 4)
     f16 = storage == tg.STORAGE_FP16
     if f16:
@@ -201,7 +201,7 @@ def test_host_api_matches_device_api(cuda_dev, storage):
 
 
 def test_reset_restarts_history(cuda_dev):
-    spec = scene.config1(64, 48, seed=10)
+    spec = scene.pan_with_disocclusion(64, 48, seed=10)
     frames = _frames(spec, 3)
     d = tg.Denoiser(64, 48)
     first = d.denoise(*(frames[0][k].to(cuda_dev) for k in KEYS)).cpu()
@@ -217,8 +217,8 @@ def test_reset_restarts_history(cuda_dev):
 def test_resize_rezeroes_state(cuda_dev, storage):
     """After resize (the reference's rebuildFrameBuffers, src/main.cpp:1547-1603) a handle behaves exactly as a
     fresh one of the new size; the caller's two outputs alternate as denoised_indirect[frame % 2]."""
-    small = _frames(scene.config1(64, 48, seed=12), 2)
-    big = _frames(scene.config1(96, 80, seed=13), 3)
+    small = _frames(scene.pan_with_disocclusion(64, 48, seed=12), 2)
+    big = _frames(scene.pan_with_disocclusion(96, 80, seed=13), 3)
     f16 = storage == tg.STORAGE_FP16
 
     def ins(fr):
@@ -247,7 +247,7 @@ def test_resize_rezeroes_state(cuda_dev, storage):
 def test_input_layouts_agree(cuda_dev):
     """RGB32F vs RGBA32F vs pitched normals and pitched radiance give identical output."""
     W, H = 48, 40
-    fr = _frames(scene.config1(W, H, seed=11), 1)[0]
+    fr = _frames(scene.pan_with_disocclusion(W, H, seed=11), 1)[0]
     rad, dep, nrm, mot = (fr[k].to(cuda_dev) for k in KEYS)
     base = tg.Denoiser(W, H).denoise(rad, dep, nrm, mot).cpu()
     nrm4 = torch.cat([nrm, torch.zeros_like(nrm[..., :1])], -1)
@@ -281,7 +281,7 @@ def test_tma_and_plain_staging_agree(cuda_dev, storage, W):
     a = tg.Denoiser(W, H, storage=storage)
     b = tg.Denoiser(W, H, storage=storage, flags=tg._lib.FLAG_NO_TMA)
     assert a.info()["tma"] == 1 and b.info()["tma"] == 0
-    sc = scene.PlaneScene(scene.config1(W, H, seed=12))
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(W, H, seed=12))
     dt = torch.float16 if f16 else torch.float32
     for t in range(6):
         fr = sc.frame(t)
@@ -307,7 +307,7 @@ def test_ref_exact_tma_and_plain_staging_agree(cuda_dev, storage, W, H, pitch_px
     a = tg.Denoiser(W, H, mode=tg.MODE_REF_EXACT, storage=storage)
     b = tg.Denoiser(W, H, mode=tg.MODE_REF_EXACT, storage=storage, flags=tg._lib.FLAG_NO_TMA)
     assert a.info()["tma"] == 1 and b.info()["tma"] == 0
-    sc = scene.PlaneScene(scene.config1(W, H, seed=13), device=cuda_dev)
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(W, H, seed=13), device=cuda_dev)
     for t in range(4):
         rad = sc.frame(t)["radiance"].to(dt)
         if pitch_px:

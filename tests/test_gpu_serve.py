@@ -14,7 +14,7 @@ KEYS = ("radiance", "depth", "normal", "motion")
 
 
 def _host_seq(w, h, frames, seed, f16=False, pinned=True):
-    sc = scene.PlaneScene(scene.config1(w, h, seed=seed))
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(w, h, seed=seed))
     seq = []
     for t in range(frames):
         fr = sc.frame(t)
@@ -133,7 +133,7 @@ def test_barrier_wait_runs_out_and_reports(cuda_dev):
     exist, every CTA gives up after 2 ms, the step reports TG_ERR_TIMEOUT and the context
     stays usable."""
     sizes = [(64, 36)]
-    sc = scene.PlaneScene(scene.config1(64, 36, seed=9))
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(64, 36, seed=9))
     fr = {k: v.to(cuda_dev) for k, v in sc.frame(0).items() if k in KEYS}
     out = [torch.empty((36, 64, 4), device=cuda_dev)]
     b = Batch(sizes, storage=tg.STORAGE_FP32, strategy=tg._lib.BATCH_PERSISTENT, barrier_timeout_us=2000,

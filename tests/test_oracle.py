@@ -230,7 +230,7 @@ def test_full_moments_are_ema_of_l_and_l2():
 def test_full_float32_agrees_with_float64():
     from tron_grid_gb300 import scene
 
-    sc = scene.PlaneScene(scene.config1(96, 64, seed=5))
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(96, 64, seed=5))
     s32 = oracle.FullState(64, 96, np.float32)
     s64 = oracle.FullState(64, 96, np.float64)
     for t in range(6):
@@ -247,7 +247,7 @@ def test_full_fp16_store_mask_decomposes():
     binary16-rounded radiance with no emulation, the empty mask equals no emulation, and True rounds every store."""
     from tron_grid_gb300 import scene
 
-    sc = scene.PlaneScene(scene.config1(64, 48, seed=7))
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(64, 48, seed=7))
     frames = [[sc.frame(t)[k].numpy() for k in ("radiance", "depth", "normal", "motion")] for t in range(4)]
     states = {k: oracle.FullState(48, 64, np.float32) for k in ("in", "pre", "none", "zero", "all", "true")}
     for rad, dep, nrm, mot in frames:

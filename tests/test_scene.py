@@ -14,7 +14,7 @@ def test_static_camera_has_zero_motion():
 
 
 def test_geometry_is_valid():
-    sc = scene.PlaneScene(scene.config1(80, 45, seed=2))
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(80, 45, seed=2))
     fr = sc.frame(0)
     assert torch.all(fr["depth"] > 0) and torch.all(torch.isfinite(fr["depth"]))
     n = fr["normal"].norm(dim=-1)
@@ -32,7 +32,7 @@ def test_noise_is_unit_mean_exponential():
 
 def test_motion_vectors_reproject_to_same_surface():
     """A pixel moved by its motion vector lands, in the previous frame, on the same plane."""
-    spec = scene.config1(160, 90, seed=4)
+    spec = scene.pan_with_disocclusion(160, 90, seed=4)
     sc = scene.PlaneScene(spec)
     prev, cur = sc.frame(9), sc.frame(10)
     H, W = 90, 160
@@ -45,7 +45,7 @@ def test_motion_vectors_reproject_to_same_surface():
 
 
 def test_plane_appears_at_frame_30():
-    spec = scene.config1(160, 90, seed=5)
+    spec = scene.pan_with_disocclusion(160, 90, seed=5)
     sc = scene.PlaneScene(spec)
     rect_id = len(sc.planes)
     assert not bool((sc.frame(29)["plane"] == rect_id).any())

@@ -48,7 +48,7 @@ def test_noalloc_matches_handle_on_two_frames(cuda_dev, storage, W, H, levels):
     params = L.default_params(L.MODE_REF_EXACT, storage, levels=levels)
     ref = tg.Denoiser(W, H, mode=L.MODE_REF_EXACT, storage=storage, levels=levels)
     moms = [torch.zeros((H, W, 2), dtype=dt, device=cuda_dev) for _ in range(2)]
-    sc = scene.PlaneScene(scene.config1(W, H, seed=21), device=cuda_dev)
+    sc = scene.PlaneScene(scene.pan_with_disocclusion(W, H, seed=21), device=cuda_dev)
     for t in range(2):
         raw = sc.frame(t)["radiance"].to(dt)
         want = torch.empty((H, W, 4), dtype=dt, device=cuda_dev)

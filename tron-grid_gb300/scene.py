@@ -40,12 +40,12 @@ class SceneSpec:
     extra: dict = field(default_factory=dict)  # {"no_emitters": True} drops the stripe emitters
 
 
-def config0(seed: int = 0) -> SceneSpec:
+def slow_pan(seed: int = 0) -> SceneSpec:
     """640x360, 8 frames, camera yaw 0.2 deg/frame."""
     return SceneSpec(640, 360, seed=seed, yaw_deg=0.2, frames=8)
 
 
-def config1(width: int = 3840, height: int = 2160, seed: int = 0) -> SceneSpec:
+def pan_with_disocclusion(width: int = 3840, height: int = 2160, seed: int = 0) -> SceneSpec:
     """60 frames, yaw 0.5 deg/frame + 0.05 m/frame translation, a plane appears at frame 30."""
     s = 0.05 / math.sqrt(2.0)
     return SceneSpec(width, height, seed=seed, yaw_deg=0.5, translation=(s, 0.0, s), appear_frame=30, frames=60)
