@@ -699,7 +699,8 @@ __device__ __forceinline__ bool ref_tma_land(const RefArgs& a, uint32_t ubar, bo
     for (int e = 0; e < (T::N + kThreads - 1) / kThreads; ++e) {
         const int k = tid + e * kThreads;
         if (k >= T::N) break;
-        const float4 c = Stor<ST>::rt4(f16_texels ? unpack_h4(reinterpret_cast<const uint2*>(land)[k]) : land[k]);
+        // binary16 texels are already in every storage format; fp32 texels are rounded to it
+        const float4 c = f16_texels ? unpack_h4(reinterpret_cast<const uint2*>(land)[k]) : Stor<ST>::rt4(land[k]);
         sA[k] = make_float4(c.x, c.y, c.z, lum(c.x, c.y, c.z));
     }
     return true;
