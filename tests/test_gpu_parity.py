@@ -174,10 +174,23 @@ def test_ref_exact_odd_sizes(cuda_dev, wh):
     _ref_pair(cuda_dev, scene.SceneSpec(wh[0], wh[1], seed=8), 4, tg.STORAGE_FP32, chk)
 
 
+def _pinned(t, pad):
+    """A pinned copy of `t` (H, W[, C]); with pad > 0 a view into rows of W + pad pixels (a pitched image)."""
+    if not pad:
+        return t.pin_memory()
+    H, W = t.shape[0], t.shape[1]
+    big = torch.zeros((H, W + pad) + tuple(t.shape[2:]), dtype=t.dtype).pin_memory()
+    v = big[:, :W]
+    v.copy_(t)
+    return v
+
+
+@pytest.mark.parametrize("pad", [0, 3])
 @pytest.mark.parametrize("storage", [tg.STORAGE_FP32, tg.STORAGE_FP16])
-def test_host_api_matches_device_api(cuda_dev, storage):
+def test_host_api_matches_device_api(cuda_dev, storage, pad):
     """tg_svgf_denoise_host (pinned host buffers, four frames through its ring of three staging sets) gives the
-    device API's bits; FP16 storage with rgba16f radiance and octahedral normals."""
+    device API's bits; FP16 storage with rgba16f radiance and octahedral normals.  pad > 0: every host image
+    (inputs and output) is pitched (rows of W + pad pixels), which the host path copies row by row."""
     spec = scene.pan_with_disocclusion(200, 120, seed=9)
     frames = _frames(spec, 4)
     f16 = storage == tg.STORAGE_FP16
@@ -190,8 +203,8 @@ def test_host_api_matches_device_api(cuda_dev, storage):
     b = tg.Denoiser(200, 120, storage=storage)
     outs_h = []
     for fr in frames:
-        ins = [fr[k].pin_memory() for k in KEYS]
-        outs_h.append(b.denoise_host(*ins, out=torch.empty((120, 200, 4), dtype=dt, pin_memory=True)))
+        ins = [_pinned(fr[k], pad) for k in KEYS]
+        outs_h.append(b.denoise_host(*ins, out=_pinned(torch.zeros((120, 200, 4), dtype=dt), pad)))
     b.synchronize()
     for fr, oh in zip(frames, outs_h):
         od = a.denoise(*(fr[k].to(cuda_dev) for k in KEYS), out=torch.empty((120, 200, 4), dtype=dt, device=cuda_dev))
