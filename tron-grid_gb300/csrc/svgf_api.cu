@@ -883,11 +883,8 @@ int tg_svgf_denoise_host(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_out
         const size_t row = size_t(fmt_bytes(hi.format)) * s->w;
         const size_t hp = hi.pitch_bytes ? size_t(hi.pitch_bytes) : row;
         *dst_imgs[k] = tg_image{sg.buf + off[k], int64_t(row), hi.format, 0};
-        // a dense image is one linear copy; a pitched one a 2-D copy
-        const cudaError_t ce = hp == row ? cudaMemcpyAsync(sg.buf + off[k], hi.ptr, row * s->h, cudaMemcpyHostToDevice,
-                                                           s->copy_stream)
-                                         : cudaMemcpy2DAsync(sg.buf + off[k], row, hi.ptr, hp, row, s->h,
-                                                             cudaMemcpyHostToDevice, s->copy_stream);
+        const cudaError_t ce =
+            copy_image_async(sg.buf + off[k], row, hi.ptr, hp, row, s->h, cudaMemcpyHostToDevice, s->copy_stream);
         if (ce != cudaSuccess) return fail(TG_ERR_CUDA, "input copy failed: %s", cudaGetErrorString(cudaGetLastError()));
     }
     if (cudaEventRecord(sg.ev_in, s->copy_stream) != cudaSuccess || cudaStreamWaitEvent(stream, sg.ev_in, 0) != cudaSuccess)
@@ -900,10 +897,8 @@ int tg_svgf_denoise_host(tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_out
     if (cudaEventRecord(sg.ev_comp, stream) != cudaSuccess || cudaStreamWaitEvent(s->d2h_stream, sg.ev_comp, 0) != cudaSuccess)
         return fail(TG_ERR_CUDA, "event record failed");
     const size_t op = out->denoised.pitch_bytes ? size_t(out->denoised.pitch_bytes) : orow;
-    const cudaError_t oe = op == orow ? cudaMemcpyAsync(out->denoised.ptr, sg.buf + off[4], orow * s->h,
-                                                         cudaMemcpyDeviceToHost, s->d2h_stream)
-                                      : cudaMemcpy2DAsync(out->denoised.ptr, op, sg.buf + off[4], orow, orow, s->h,
-                                                          cudaMemcpyDeviceToHost, s->d2h_stream);
+    const cudaError_t oe =
+        copy_image_async(out->denoised.ptr, op, sg.buf + off[4], orow, orow, s->h, cudaMemcpyDeviceToHost, s->d2h_stream);
     if (oe != cudaSuccess) return fail(TG_ERR_CUDA, "output copy failed: %s", cudaGetErrorString(cudaGetLastError()));
     if (cudaEventRecord(sg.ev_done, s->d2h_stream) != cudaSuccess) return fail(TG_ERR_CUDA, "event record failed");
     sg.used = true;

@@ -637,8 +637,7 @@ void scheduler(tg_svgf_server* sv)
                     s.in_view[q] = tg_image{dv, int64_t(hp), s.fmt[q], 0};
                     continue;
                 }
-                cudaMemcpy2DAsync(s.in_slot[slot][q], row, src[q]->ptr, hp, row, s.h, cudaMemcpyHostToDevice,
-                                  sv->s_h2d);
+                copy_image_async(s.in_slot[slot][q], row, src[q]->ptr, hp, row, s.h, cudaMemcpyHostToDevice, sv->s_h2d);
                 s.in_view[q] = tg_image{s.in_slot[slot][q], 0, s.fmt[q], 0};
                 copied = true;
             }
@@ -674,8 +673,7 @@ void scheduler(tg_svgf_server* sv)
             const int slot = int(s.frames & 1u);
             const size_t row = size_t(fmt_bytes(s.fmt[4])) * s.w;
             const size_t op = r->out.denoised.pitch_bytes ? size_t(r->out.denoised.pitch_bytes) : row;
-            cudaMemcpy2DAsync(r->out.denoised.ptr, op, s.out_slot[slot], row, row, s.h, cudaMemcpyDeviceToHost,
-                              sv->s_d2h);
+            copy_image_async(r->out.denoised.ptr, op, s.out_slot[slot], row, row, s.h, cudaMemcpyDeviceToHost, sv->s_d2h);
             s.frames++;
             r->t_launch = tl;
             r->batch_size = uint32_t(batch.size());
