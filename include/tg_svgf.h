@@ -175,7 +175,9 @@ TG_API int tg_svgf_denoise(tg_svgf* h, const tg_svgf_inputs* inputs, const tg_sv
  * The copies run on the handle's own streams, so the caller keeps the host
  * buffers alive and unmodified until tg_svgf_synchronize returns.  Host
  * buffers should be page-locked for the copies to overlap with compute; the
- * staging is a ring of three sets, so up to three frames are in flight. */
+ * staging is a ring of three sets, so up to three frames are in flight.  A
+ * dense image (pitch_bytes 0 or equal to the row) moves by one linear copy,
+ * which is markedly faster than the row-by-row copy a padded pitch needs. */
 TG_API int tg_svgf_denoise_host(tg_svgf* h, const tg_svgf_inputs* host_inputs, const tg_svgf_outputs* host_outputs,
                          void* stream);
 
