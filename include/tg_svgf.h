@@ -245,7 +245,7 @@ typedef struct tg_svgf_batch_desc {
     const uint32_t* heights;   /* n_streams heights */
     tg_svgf_params params;     /* mode must be TG_SVGF_MODE_FULL */
     int32_t device;            /* -1 = current */
-    int32_t rows_per_thread;   /* a-trous outputs per thread (tile 32 x 8r): 1 or 2; 0 = 2 until autotuned */
+    int32_t rows_per_thread;   /* a-trous outputs per thread (tile 32 x 4r): 1 or 2; 0 = 2 until autotuned */
     int32_t ctas_per_sm;       /* persistent CTAs per SM: 1..3; 0 = the occupancy limit */
     int32_t use_graph;         /* nonzero: replay each step from a captured CUDA graph */
     int32_t strategy;          /* TG_SVGF_BATCH_STAGES (default) or TG_SVGF_BATCH_PERSISTENT */

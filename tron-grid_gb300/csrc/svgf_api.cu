@@ -353,11 +353,11 @@ EncodeTiledFn encode_tiled()
 
 // One tensor map per a-trous level L >= 1 over that level's input records in
 // the residue-major layout of stride 2^L: {float, row, plane, half-plane};
-// box = one 36 x 20 halo tile, whose rows are contiguous lines.
+// box = one 36 x (4R + 4) halo tile, whose rows are contiguous lines.
 // Level 0 has no records: its maps cover the tc and guide planes.
 // REF_EXACT: a 3-D map {texel, row, plane} over pass L's input (residue-major
 // planes of stride 2^L; 8-byte texels of fp16 images as UINT64, 16-byte ones as
-// 4 floats), box = one 36 x 20 halo tile of one plane.  A level whose plane
+// 4 floats), box = one 36 x (4R + 4) halo tile of one plane.  A level whose plane
 // rows are not a multiple of 16 bytes stages with plain loads.
 void build_ref_maps(tg_svgf* s, EncodeTiledFn enc)
 {
@@ -509,7 +509,7 @@ int check_inputs(const tg_svgf* s, const tg_svgf_inputs* in, const tg_svgf_outpu
 namespace tg {
 
 // TMA maps of a FULL stream's a-trous levels for tiles of R output rows per
-// thread (box = 36 x (8R + 4) cells); see svgf_internal.h for the layout and
+// thread (box = 36 x (4R + 4) cells); see svgf_internal.h for the layout and
 // the mask.  Each map's preconditions (16-byte strides and base) are those of
 // cuTensorMapEncodeTiled; a level whose map cannot be encoded stages with plain
 // loads.

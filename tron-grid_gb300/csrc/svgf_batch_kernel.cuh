@@ -3,7 +3,7 @@
 // loop (svgf_serve.cu).
 //
 // Work-list.  A step has 2 + L stages (temporal, variance, L a-trous levels).
-// Stage k of stream j is cut into tiles (32 x 8 pixels for the pixel stages, a
+// Stage k of stream j is cut into tiles (32 x 4 pixels for the pixel stages, a
 // residue-class tile for the levels, exactly as in the single-stream kernels);
 // the work table holds, per stage, the exclusive prefix sum of the tile counts
 // over the active streams.  Every CTA of the persistent grid takes items
@@ -122,7 +122,7 @@ static_assert(kLvTX == kBlockX && kLvRows == kBlockY, "pixel and level CTAs must
 static_assert(sizeof(VarTile) <= sizeof(LevelSmem<1>), "K2 tile must fit the level tile");
 
 template <int ST, int R>
-__global__ void __launch_bounds__(kLvTX* kLvRows, 3) k_batch_step(const char* __restrict__ table, int cap,
+__global__ void __launch_bounds__(kLvTX* kLvRows, 6) k_batch_step(const char* __restrict__ table, int cap,
                                                                    BarrierState* bar, unsigned expect_blocks,
                                                                    long long spin_cycles)
 {

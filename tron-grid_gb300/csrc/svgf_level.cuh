@@ -35,7 +35,7 @@
 namespace tg {
 
 constexpr int kLvTX = 32;      // outputs per tile row (one warp)
-constexpr int kLvRows = 8;     // thread rows per CTA
+constexpr int kLvRows = 4;     // thread rows per CTA
 constexpr float kLog2e = kLog2eF;
 // log2 of the B3 taps 1/16, 1/4, 3/8, 1/4, 1/16.
 __device__ __forceinline__ constexpr float log2_b3(int i)
@@ -60,11 +60,12 @@ template <int R> struct LevelTile {
     static constexpr int N = SW * SH;
 };
 
-// CTAs per SM the level kernels are compiled for: at R = 2 four CTAs (32
-// warps, 64 registers a thread) hide the tap loop's latencies better than
-// three with 80 registers.
+// CTAs per SM the level kernels are compiled for: at R = 2 eight CTAs of 128
+// threads (32 warps, 64 registers a thread) hide the tap loop's latencies and
+// the tile waits better than four of 256 threads (2% slower per level), two of
+// 512 (15% slower) or 256-thread CTAs at 80 registers.
 template <int R> struct LevelOcc {
-    static constexpr int kCtas = R <= 2 ? 4 : 2;
+    static constexpr int kCtas = R <= 2 ? 8 : 4;
 };
 
 // Staged tile of one level: X0 = (r, g, b, variance), X1 = (unit normal, depth),
@@ -397,7 +398,7 @@ __global__ void __launch_bounds__(kLvTX* kLvRows, LevelOcc<R>::kCtas) k_full_lev
 // one elected thread issues cp.async.bulk.tensor for the tile's box of
 // residue-major records (a 4-D map {float, row, plane, half-plane}, so that the
 // box of each half lands as one dense float4 array and each tile row is one
-// contiguous 576-byte line); level 0 reads two 2-D maps over the tc and guide
+// contiguous line of 36 records); level 0 reads two 2-D maps over the tc and guide
 // planes instead.  Completion is tracked by an mbarrier transaction count and
 // cells outside the plane array arrive zero-filled.  The wait is bounded: a box
 // that has not landed after about a second sets a->err, the CTA waits (bounded)
@@ -802,11 +803,12 @@ __device__ __forceinline__ void ref_first_tile(const RefArgs& a, int i0, int j0,
     ref_taps_out<ST, R>(a, 1, 0, 0, i0, j0, ca, valid, sA);
 }
 
-// CTAs per SM the REF_EXACT kernels are compiled for: 6 (40 registers a
-// thread, 48 warps) measured 14% faster per 4K frame than the 5 that 42
-// registers allowed; 3 rows per thread (28 rows staged per 24) was slower.
+// CTAs per SM the REF_EXACT kernels are compiled for: 12 of 128 threads (40
+// registers a thread, 48 warps).  48 warps measured 14% faster per 4K frame
+// than the 40 that 42 registers allowed; 12 CTAs of 128 threads ran as fast as
+// 6 of 256; 3 rows per thread was slower.
 #ifndef TG_REF_CTAS
-#define TG_REF_CTAS 6
+#define TG_REF_CTAS 12
 #endif
 #ifndef TG_REF_FIRST_CTAS
 #define TG_REF_FIRST_CTAS TG_REF_CTAS
