@@ -69,9 +69,12 @@ template <int R> struct LevelOcc {
 };
 
 // Staged tile of one level: X0 = (r, g, b, variance), X1 = (unit normal, depth),
-// XL = luminance.  X0 and X1 are 128-byte aligned so that a TMA box can land in
-// them directly (N * 16 bytes is a multiple of 128 for every tile shape used).
+// XL = luminance.  A TMA box must land on a 128-byte boundary: X0 and X1 start
+// on one (N * 16 bytes is a multiple of 128), and so does the second half of
+// X1, where a binary16 level-0 tile lands its guide box (N * 8 bytes in).
 template <int R> struct __align__(128) LevelSmem {
+    static_assert((LevelTile<R>::N * 8) % 128 == 0,
+                  "every TMA destination in a level tile must start on a 128-byte boundary");
     float4 X0[LevelTile<R>::N];
     float4 X1[LevelTile<R>::N];
     float XL[LevelTile<R>::N];
