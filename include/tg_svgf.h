@@ -246,7 +246,7 @@ typedef struct tg_svgf_batch_desc {
     tg_svgf_params params;     /* mode must be TG_SVGF_MODE_FULL */
     int32_t device;            /* -1 = current */
     int32_t rows_per_thread;   /* a-trous outputs per thread (tile 32 x 4r): 1 or 2; 0 = 2 until autotuned */
-    int32_t ctas_per_sm;       /* persistent CTAs per SM: 1..3; 0 = the occupancy limit */
+    int32_t ctas_per_sm;       /* persistent CTAs (of 128 threads) per SM, up to the occupancy limit; 0 = that limit */
     int32_t use_graph;         /* nonzero: replay each step from a captured CUDA graph */
     int32_t strategy;          /* TG_SVGF_BATCH_STAGES (default) or TG_SVGF_BATCH_PERSISTENT */
     uint32_t barrier_timeout_us; /* bound of each grid-barrier wait; 0 = about one second */
@@ -256,7 +256,7 @@ typedef struct tg_svgf_batch_desc {
 
 typedef struct tg_svgf_batch_info {
     uint32_t n_streams;
-    int32_t rows_per_thread;   /* current tile shape: 32 x (8 * rows_per_thread) outputs */
+    int32_t rows_per_thread;   /* current tile shape: 32 x (4 * rows_per_thread) outputs */
     int32_t ctas_per_sm;
     int32_t grid_ctas;         /* persistent grid size */
     int32_t graphs;            /* 1 when steps replay CUDA graphs */

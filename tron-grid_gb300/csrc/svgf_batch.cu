@@ -570,10 +570,11 @@ int tg_svgf_batch_autotune(tg_svgf_batch* b, uint32_t n, const uint32_t* ids, co
     double best = 1e30;
     int bestR = b->R, bestC = b->ctas, bestS = b->strategy;
     for (int cand = 0; cand < 2 * (1 + 3) && st == TG_OK; ++cand) {
-        // candidates: (stages, R) for R = 1, 2, then (persistent, R, ctas) up to the occupancy limit
+        // candidates: (stages, R) for R = 1, 2, then (persistent, R, ctas) with 2, 4 or 6 CTAs of 128 threads
+        // per SM, up to the occupancy limit
         const int strat = cand < 2 ? TG_SVGF_BATCH_STAGES : TG_SVGF_BATCH_PERSISTENT;
         const int R = cand < 2 ? cand + 1 : 1 + (cand - 2) / 3;
-        const int c = cand < 2 ? 0 : 1 + (cand - 2) % 3;
+        const int c = cand < 2 ? 0 : 2 * (1 + (cand - 2) % 3);
         if (strat == TG_SVGF_BATCH_PERSISTENT && c > max_ctas_per_sm(f16, R)) continue;
         if ((st = set_config(b, strat, R, c))) break;
         if ((st = run_step(b, n, ids, in, out, stream)) != TG_OK) break;  // warm-up, also captures
